@@ -1,0 +1,316 @@
+"""Benchmark: batched friction-contact QP solves per second on GB300.
+
+Workload (one step): 4096 independent friction-contact QPs, c ~ U{4..64} contacts each
+(n = 3c forces, m = 4c cone rows: R^c_+ x c Q^3), solved to the 1e-8 relative gap by one
+batched mixed-precision (FP32 factor, FP64 refinement) launch sequence. Synthetic, seeded data
+of the reference's contact-problem shape; cold starts (warm_start off) so every step repeats
+the full solve. Inputs stay resident in HBM (they exceed the 129 MB L2, so no flush is needed).
+
+  value  -- solves/s of the device-resident batch (CUDA events on the solver's stream)
+  e2e    -- the same through the C-ABI with pinned HOST buffers: H2D of the step's values,
+            solve, D2H of x, s, z inside the timed region
+  cpu_baseline -- the FP64 CPU restatement of the reference (oracle, "port") on the host cores,
+            one instance per thread, on a bounded sample
+  plain_gpu -- the plain per-instance GPU form (FP64 factor, one launch per solve)
+
+`--impl reference` times the reference's CPU path (the oracle port; the reference itself cannot
+be built here) on the same workload with every host thread.
+Multi-GPU: one process per GPU (torchrun); each rank solves its own 4096-instance batch (weak
+scaling, no data-path collective); the reported time is the max over ranks.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "QP solves/s at 1e-8 rel. gap: batched mixed-prec vs plain GPU vs host CPU; fwd+bwd µs"
+WORKLOAD = "batched friction-contact QPs: 4096 instances, c~U{4..64}, n=3c, cones R^c_+ x c Q^3, mixed FP32/FP64"
+COUNT = 4096
+
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d.get("hbm_gbs", 6800.0)), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self._t = threading.Thread(target=self._read, daemon=True)
+            self._t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for nm, flag in zip(names, parts[5:9]):
+                if flag.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def run_gb300(args, rank, world, local_rank):
+    import torch
+
+    from conicxx_gb300 import BatchSolver, Solver, default_settings, generators
+    from conicxx_gb300._abi import INFO_DTYPE
+
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    qps = generators.contact_batch(COUNT, base_seed=rank * COUNT)
+    st = default_settings(precision=1, warm_start=0)
+    t0 = time.perf_counter()
+    B = BatchSolver(qps, settings=st)
+    setup_s = time.perf_counter() - t0
+    Px, q, Ax, b = B.concat_values()
+    dvals = [torch.from_numpy(v).to(dev) for v in (Px, q, Ax, b)]
+    dx = torch.empty(B.n_total, dtype=torch.float64, device=dev)
+    ds = torch.empty(B.m_total, dtype=torch.float64, device=dev)
+    dz = torch.empty(B.m_total, dtype=torch.float64, device=dev)
+    stream = torch.cuda.Stream(device=dev)
+    sp = stream.cuda_stream
+
+    def step():
+        B.update_values_device(*(int(t.data_ptr()) for t in dvals), sp)
+        B.solve_device(int(dx.data_ptr()), int(ds.data_ptr()), int(dz.data_ptr()), sp)
+
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            step()
+    torch.cuda.synchronize()
+    launches_per_step = B.last_launches()
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+
+            dist.barrier()
+
+    sampler = ClockSampler(local_rank)
+    sampler.start()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    barrier()
+    torch.cuda.synchronize()
+    w0 = time.perf_counter()
+    with torch.cuda.stream(stream):
+        for i in range(args.steps):
+            evs[i][0].record(stream)
+            step()
+            evs[i][1].record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    wall = time.perf_counter() - w0
+    clocks = sampler.stop()
+    step_ms = np.array([a.elapsed_time(b_) for a, b_ in evs])
+    ms_local = float(step_ms.mean())
+    ms = ms_local
+    if world > 1:
+        import torch.distributed as dist
+
+        t = torch.tensor([ms_local], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    infos = np.zeros(COUNT, dtype=INFO_DTYPE)
+    B.solve_device(int(dx.data_ptr()), int(ds.data_ptr()), int(dz.data_ptr()), sp, infos)
+    solved_frac = float(np.mean(infos["status"] == 1))
+    statuses = {int(k): int(v) for k, v in zip(*np.unique(infos["status"], return_counts=True))}
+
+    result = {}
+    if rank == 0:
+        # ---- e2e through the C-ABI with pinned host buffers ----
+        pin = lambda a: torch.from_numpy(a).pin_memory().numpy()  # noqa: E731
+        hvals = [pin(v) for v in (Px, q, Ax, b)]
+        hx, hs, hz = (pin(np.zeros(k)) for k in (B.n_total, B.m_total, B.m_total))
+        from conicxx_gb300._abi import dptr
+        from conicxx_gb300._lib import check, lib
+
+        L = lib()
+
+        def e2e_step():
+            check(L.cxg_batch_update_values(B._h, *(dptr(v) for v in hvals)), "update")
+            check(L.cxg_batch_solve(B._h, dptr(hx), dptr(hs), dptr(hz), None), "solve")
+
+        for _ in range(max(1, args.warmup // 2)):
+            e2e_step()
+        e0 = time.perf_counter()
+        e2e_steps = max(2, args.steps)
+        for _ in range(e2e_steps):
+            e2e_step()
+        e2e_s = (time.perf_counter() - e0) / e2e_steps
+        h2d = 8 * (B.nnzP + B.n_total + B.nnzA + B.m_total)
+        d2h = 8 * (B.n_total + 2 * B.m_total)
+        # ---- plain per-instance GPU form (FP64 factor, one solve per launch) ----
+        plain_n = args.plain_instances
+        sub = qps[:plain_n]
+        solvers = []
+        for qp in sub:
+            S = Solver()
+            assert S.setup(qp, warm_start=0)
+            solvers.append(S)
+        solvers[0].solve()
+        p0 = time.perf_counter()
+        for S in solvers:
+            S.solve()
+        plain_s = time.perf_counter() - p0
+        plain_rate = plain_n / plain_s
+        # ---- CPU baseline: oracle restatement on the host cores ----
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle as orc
+
+        orc.build()
+        ncpu = os.cpu_count() or 1
+        sample = qps[:args.cpu_sample]
+        cpu_wall, cpu_st, _ = orc.batch_solve(sample, ncpu, warm_start=0)
+        cpu_rate = len(sample) / cpu_wall
+        # ---- roofline of the IPM kernel (the only kernel of the timed region) ----
+        hbm_peak, peak_kind = peaks()
+        algo_bytes = B.algorithmic_bytes()
+        achieved = algo_bytes / (ms * 1e-3) / 1e9
+        traffic = None
+        tp = os.path.join(ROOT, "profiles", "ipm_kernel_traffic.json")
+        if os.path.exists(tp):
+            with open(tp) as f:
+                traffic = json.load(f).get("dram_bytes_per_launch_4096")
+        result = dict(
+            e2e={"value": COUNT / e2e_s, "unit": "solves/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+            plain_gpu={"value": plain_rate, "unit": "solves/s", "instances": plain_n, "precision": "fp64",
+                       "batched_over_plain": (COUNT / (ms * 1e-3)) / plain_rate},
+            cpu_baseline={"value": cpu_rate, "unit": "solves/s", "cores": ncpu, "kind": "port",
+                          "sample": f"first {len(sample)} of the 4096 instances, one instance per thread, "
+                                    f"cold start, FP64 oracle restatement of the reference",
+                          "solved_fraction": float(np.mean(cpu_st == 1))},
+            roofline={"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                      "frac": achieved / hbm_peak, "traffic": traffic, "peak_kind": peak_kind,
+                      "note": "IPM kernel; HBM bytes = problem data + plans + solutions per launch; the kernel "
+                              "is bound by the FP64 pipe and barrier latency, not HBM (see profiles/)"},
+            setup_s=setup_s,
+        )
+    return ms, wall, clocks, launches_per_step, solved_frac, statuses, result
+
+
+def run_reference(args, rank, world):
+    """The reference's CPU path: the FP64 oracle restatement (the reference itself cannot be
+    built in this environment), all host threads, one instance per thread."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as orc
+    from conicxx_gb300 import generators
+
+    if rank != 0:
+        return None
+    orc.build()
+    qps = generators.contact_batch(COUNT)
+    ncpu = os.cpu_count() or 1
+    sample = args.cpu_sample
+    rates = []
+    for i in range(args.warmup + args.steps):
+        lo = (i * sample) % COUNT
+        sub = qps[lo:lo + sample]
+        wall, st, _ = orc.batch_solve(sub, ncpu, warm_start=0)
+        if i >= args.warmup:
+            rates.append(len(sub) / wall)
+    value = float(np.mean(rates))
+    return {
+        "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * sample / value, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded contact generator)",
+        "config": {"workload": WORKLOAD, "count": COUNT, "sample_per_step": sample},
+        "impl": "reference",
+        "cpu_baseline": {"value": value, "unit": "solves/s", "cores": ncpu, "kind": "port",
+                         "sample": f"{sample} instances per step, one instance per thread, cold start"},
+        "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--cpu-sample", type=int, default=1024)
+    ap.add_argument("--plain-instances", type=int, default=16)
+    args = ap.parse_args()
+    rank, world, local_rank = dist_env()
+    if args.impl == "reference":
+        out = run_reference(args, rank, world)
+        if out is not None:
+            print(json.dumps(out), flush=True)
+        return
+    if not os.path.exists(os.path.join(ROOT, "conicxx_gb300", "_build", "libconicxx_gb300.so")):
+        import __graft_entry__
+
+        __graft_entry__.build()
+    ms, wall, clocks, launches, solved_frac, statuses, extra = run_gb300(args, rank, world, local_rank)
+    if rank == 0:
+        out = {
+            "metric": METRIC, "value": world * COUNT / (ms * 1e-3), "unit": "solves/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "mixed fp32-factor/fp64",
+            "data": "synthetic (seeded contact generator)",
+            "config": {"workload": WORKLOAD, "count_per_gpu": COUNT, "parallelism": f"instances x{world}",
+                       "l2": "inputs resident in HBM exceed the 129 MB L2; no flush",
+                       "solved_fraction": solved_frac, "statuses": statuses, "warm_start": False},
+            "wall_s_timed_region": wall, "gpu_launches": launches * args.steps, "clocks": clocks,
+        }
+        out.update(extra)
+        print(json.dumps(out), flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,747 @@
+// C-ABI of the GB300 ConicXX path (declared in include/conicxx_gb300.h).
+//
+// cxg_batch: N independent instances; one persistent launch per size bucket, instances taken
+// heaviest-first from an atomic queue; the device-side sequence (queue resets + launches) is
+// captured once into a CUDA graph and replayed on every solve.
+// cxg_solver: conicxx::Solver semantics (include/conicxx/solver.h) over a batch of one, FP64
+// factorisation by default (the plain per-instance GPU form).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "conicxx_gb300.h"
+#include "cxg_kernels.h"
+#include "cxg_layout.h"
+#include "cxg_plan.h"
+
+using namespace cxg;
+
+static thread_local std::string g_lastError;
+
+namespace cxg {
+std::string& lastErrorRef() { return g_lastError; }
+}  // namespace cxg
+
+static int setErr(int code, const std::string& msg) {
+  g_lastError = msg;
+  return code;
+}
+
+#define CX_CUDA(call)                                                                        \
+  do {                                                                                       \
+    cudaError_t e_ = (call);                                                                 \
+    if (e_ != cudaSuccess)                                                                   \
+      return setErr(CXG_E_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));         \
+  } while (0)
+
+extern "C" const char* cxg_last_error(void) { return g_lastError.c_str(); }
+extern "C" const char* cxg_version(void) { return "conicxx_gb300 0.1.0"; }
+
+extern "C" int cxg_device_count(void) {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return n;
+}
+
+extern "C" const char* cxg_status_string(int status) {
+  switch (status) {
+    case CXG_STATUS_UNSOLVED: return "Unsolved";
+    case CXG_STATUS_SOLVED: return "Solved";
+    case CXG_STATUS_PRIMAL_INFEASIBLE: return "PrimalInfeasible";
+    case CXG_STATUS_DUAL_INFEASIBLE: return "DualInfeasible";
+    case CXG_STATUS_MAX_ITERATIONS: return "MaxIterations";
+    case CXG_STATUS_NUMERICAL_ERROR: return "NumericalError";
+  }
+  return "Unknown";
+}
+
+extern "C" void cxg_default_settings(cxg_settings* s) {
+  if (!s) return;
+  std::memset(s, 0, sizeof(*s));
+  s->tol_feas = 1e-8;
+  s->tol_gap_abs = 1e-8;
+  s->tol_gap_rel = 1e-8;
+  s->tol_infeas = 1e-7;
+  s->max_iter = 200;
+  s->static_reg_P = 1e-8;
+  s->static_reg_A = 1e-8;
+  s->dynamic_reg_eps = 1e-14;
+  s->dynamic_reg_delta = 1e-7;
+  s->refine_max_iter = 3;
+  s->refine_tol = 1e-12;
+  s->max_step_fraction = 0.99;
+  s->equilibrate = 1;
+  s->equilibrate_max_iter = 10;
+  s->equilibrate_min_scale = 1e-4;
+  s->equilibrate_max_scale = 1e4;
+  s->warm_start = 1;
+  s->verbose = 0;
+  s->record_timings = 0;
+  s->validate_inputs = 1;
+  s->linear_solver = CXG_LINSOLVER_QDLDL;
+  s->precision = CXG_PRECISION_FP64;
+  s->mixed_refine_max_iter = 6;
+  s->mixed_fallback_tol = 1e-10;
+  s->threads_per_instance = 0;
+}
+
+// ------------------------------------------------------------------------------------------
+// batch
+// ------------------------------------------------------------------------------------------
+struct Group {
+  int begin = 0, count = 0;  // range in `order`
+  int block = 128, grid = 1;
+  bool fp32 = false;
+  SmemLayout lay{};
+  size_t smem = 0;
+  int64_t stride = 0;        // scratch doubles per CTA
+  int64_t scratchOff = 0;    // offset of this group's scratch in the batch scratch buffer
+  int counterIdx = 0;
+};
+
+struct cxg_batch {
+  int count = 0;
+  cxg_settings st{};      // current settings
+  cxg_settings kktSt{};   // KKT fields frozen at setup (kkt_system.cpp:26-31)
+  Pools pools;
+  std::vector<std::vector<int>> Pp, Pi, Ap, Ai;  // patterns for updateData checks
+  std::vector<int> order;
+  std::vector<Group> groups;
+  // device
+  InstanceDesc* dDesc = nullptr;
+  int* dIpool = nullptr;
+  double* dDpool = nullptr;
+  double *dPx = nullptr, *dq = nullptr, *dAx = nullptr, *db = nullptr;
+  double *dx = nullptr, *ds = nullptr, *dz = nullptr;
+  DevResult* dRes = nullptr;
+  double *dWx = nullptr, *dWs = nullptr, *dWz = nullptr;
+  unsigned char* dHaveWarm = nullptr;
+  double* dScratch = nullptr;
+  int* dCounters = nullptr;
+  int* dOrder = nullptr;
+  cudaStream_t stream = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t graphExec = nullptr;
+  DevSettings graphSettings{};
+  bool graphValid = false;
+  std::vector<DevResult> hRes;
+  int lastLaunches = 0;
+  double setupTime = 0.0;
+  int device = 0;
+
+  ~cxg_batch() {
+    if (graphExec) cudaGraphExecDestroy(graphExec);
+    if (graph) cudaGraphDestroy(graph);
+    void* ptrs[] = {dDesc, dIpool, dDpool, dPx, dq, dAx, db, dx, ds, dz, dRes, dWx, dWs, dWz, dHaveWarm, dScratch, dCounters, dOrder};
+    for (void* p : ptrs)
+      if (p) cudaFree(p);
+    if (stream) cudaStreamDestroy(stream);
+  }
+};
+
+static DevSettings makeDevSettings(const cxg_settings& st, const cxg_settings& kk) {
+  DevSettings d{};
+  d.tol_feas = st.tol_feas;
+  d.tol_gap_abs = st.tol_gap_abs;
+  d.tol_gap_rel = st.tol_gap_rel;
+  d.tol_infeas = st.tol_infeas;
+  d.static_reg_P = kk.static_reg_P;
+  d.static_reg_A = kk.static_reg_A;
+  d.dynamic_reg_eps = kk.dynamic_reg_eps;
+  d.dynamic_reg_delta = kk.dynamic_reg_delta;
+  d.refine_tol = kk.refine_tol;
+  d.max_step_fraction = st.max_step_fraction;
+  d.mixed_fallback_tol = st.mixed_fallback_tol;
+  d.max_iter = st.max_iter;
+  d.refine_max_iter = kk.refine_max_iter;
+  d.mixed_refine_max_iter = std::max(st.mixed_refine_max_iter, 0);
+  d.linear_solver = kk.linear_solver;
+  d.equilibrate = kk.equilibrate;
+  d.warm_start = st.warm_start;
+  d.precision = st.precision;
+  d.record_timings = st.record_timings ? 1 : 0;
+  return d;
+}
+
+static bool sameDev(const DevSettings& a, const DevSettings& b) { return std::memcmp(&a, &b, sizeof(a)) == 0; }
+
+template <typename T>
+static int devAlloc(T** p, size_t count) {
+  if (count == 0) count = 1;
+  cudaError_t e = cudaMalloc((void**)p, count * sizeof(T));
+  if (e != cudaSuccess) return setErr(CXG_E_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+  return CXG_OK;
+}
+
+static int64_t r2(int64_t v) { return (v + 1) & ~int64_t(1); }
+
+// Group boundaries on the root dimension nr; each group gets a shared-memory layout sized for
+// its largest instance.
+static const int kBucketEdges[] = {48, 96, 144, 192, 256, 384, 512, 1024, 2048, 4096};
+
+static int chooseBlock(int nrMax, int requested) {
+  if (requested == 64 || requested == 128 || requested == 256 || requested == 512) return requested;
+  if (nrMax <= 96) return 128;
+  if (nrMax <= 512) return 256;
+  return 512;
+}
+
+static int buildGroups(cxg_batch* B) {
+  const int N = B->count;
+  const bool fp32 = B->st.precision == CXG_PRECISION_MIXED;
+  int dev = 0;
+  CX_CUDA(cudaGetDevice(&dev));
+  B->device = dev;
+  int smemOptin = 0, numSM = 0;
+  CX_CUDA(cudaDeviceGetAttribute(&smemOptin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  CX_CUDA(cudaDeviceGetAttribute(&numSM, cudaDevAttrMultiProcessorCount, dev));
+  const size_t fixedSmem = 1024;  // static __shared__ (Ctx, queue slot) and alignment slack
+  // order: by bucket (descending nr), then by cost descending
+  std::vector<int> idx((size_t)N);
+  std::iota(idx.begin(), idx.end(), 0);
+  auto bucketOf = [&](int nr) {
+    int b = 0;
+    for (int e : kBucketEdges) {
+      if (nr <= e) return b;
+      ++b;
+    }
+    return b;
+  };
+  std::stable_sort(idx.begin(), idx.end(), [&](int a, int b) {
+    const int ba = bucketOf(B->pools.desc[(size_t)a].nr), bb = bucketOf(B->pools.desc[(size_t)b].nr);
+    if (ba != bb) return ba > bb;
+    return B->pools.desc[(size_t)a].cost > B->pools.desc[(size_t)b].cost;
+  });
+  B->order = idx;
+  B->groups.clear();
+  int64_t scratchTotal = 0;
+  for (int s = 0; s < N;) {
+    int e = s;
+    const int bk = bucketOf(B->pools.desc[(size_t)idx[(size_t)s]].nr);
+    while (e < N && bucketOf(B->pools.desc[(size_t)idx[(size_t)e]].nr) == bk) ++e;
+    Group g;
+    g.begin = s;
+    g.count = e - s;
+    g.fp32 = fp32;
+    SmemLayout& L = g.lay;
+    L.nMax = L.mMax = L.nrMax = L.nsocMax = 0;
+    for (int t = s; t < e; ++t) {
+      const InstanceDesc& D = B->pools.desc[(size_t)idx[(size_t)t]];
+      L.nMax = std::max(L.nMax, D.n);
+      L.mMax = std::max(L.mMax, D.m);
+      L.nrMax = std::max(L.nrMax, D.nr);
+      L.nsocMax = std::max(L.nsocMax, D.nsoc);
+    }
+    const int64_t redBytes = (128 + 32) * 8;
+    const int64_t vecBytes = vecDoubles(L.nMax, L.mMax, L.nrMax, L.nsocMax) * 8;
+    const int64_t root32Bytes = rootSize(L.nrMax) * 4, root64Bytes = rootSize(L.nrMax) * 8;
+    const int64_t budget = (int64_t)smemOptin - (int64_t)fixedSmem;
+    L.redOff = 0;
+    L.vecOff = redBytes;
+    L.vecInSmem = (redBytes + vecBytes <= budget) ? 1 : 0;
+    int64_t used = redBytes + (L.vecInSmem ? vecBytes : 0);
+    used = (used + 15) & ~int64_t(15);
+    L.rootOff = used;
+    // FP64 root (FP64 precision, or the mixed-precision fallback) in shared memory when it fits;
+    // the FP32 root then shares that region.
+    L.rootInSmem = 0;
+    L.root64InSmem = 0;
+    if (used + root64Bytes <= budget) {
+      L.rootInSmem = 1;
+      L.root64InSmem = 1;
+      used += root64Bytes;
+    } else if (fp32 && used + root32Bytes <= budget) {
+      L.rootInSmem = 1;
+      used += root32Bytes;
+    }
+    L.total = used;
+    g.smem = (size_t)used;
+    g.block = chooseBlock(L.nrMax, B->st.threads_per_instance);
+    // per-instance scratch layout (relative to the CTA base); the FP64 root is needed when the
+    // root is not in shared memory (FP64 precision) or for the mixed-precision fallback.
+    const bool needRoot64 = !L.root64InSmem;
+    int64_t stride = 0;
+    for (int t = s; t < e; ++t) {
+      InstanceDesc& D = B->pools.desc[(size_t)idx[(size_t)t]];
+      int64_t o = 0;
+      D.sPv = o; o += r2((int64_t)D.nnzPu + D.nnzPs);
+      D.sAv = o; o += r2(D.nnzA);
+      D.sAd = o; o += r2(D.nAd);
+      D.sT = o; o += r2(D.nAd);
+      D.sQ = o; o += r2(D.n);
+      D.sB = o; o += r2(D.m);
+      D.sRoot64 = o; o += needRoot64 ? r2(rootSize(D.nr)) : 0;
+      D.sVec = o; o += L.vecInSmem ? 0 : vecDoubles(L.nMax, L.mMax, L.nrMax, L.nsocMax);
+      D.scratchDoubles = o;
+      stride = std::max(stride, o);
+    }
+    g.stride = std::max<int64_t>(r2(stride), 2);
+    // persistent grid: resident CTAs for this configuration, capped by the group size
+    int occ = 0;
+    const cudaError_t oe = ipmOccupancy(&occ, g.block, g.smem, fp32);
+    if (oe != cudaSuccess || occ < 1) occ = 1;
+    g.grid = std::max(1, std::min(g.count, occ * numSM));
+    g.scratchOff = scratchTotal;
+    scratchTotal += g.stride * g.grid;
+    g.counterIdx = (int)B->groups.size();
+    B->groups.push_back(g);
+    s = e;
+  }
+  // scratch
+  if (B->dScratch) cudaFree(B->dScratch);
+  B->dScratch = nullptr;
+  int rc = devAlloc(&B->dScratch, (size_t)std::max<int64_t>(scratchTotal, 2));
+  if (rc) return rc;
+  return CXG_OK;
+}
+
+static int uploadPlan(cxg_batch* B) {
+  const size_t N = (size_t)B->count;
+  int rc;
+  if ((rc = devAlloc(&B->dDesc, N))) return rc;
+  if ((rc = devAlloc(&B->dIpool, B->pools.ipool.size()))) return rc;
+  if ((rc = devAlloc(&B->dDpool, B->pools.dpool.size()))) return rc;
+  if ((rc = devAlloc(&B->dPx, (size_t)B->pools.totPx))) return rc;
+  if ((rc = devAlloc(&B->dq, (size_t)B->pools.totQ))) return rc;
+  if ((rc = devAlloc(&B->dAx, (size_t)B->pools.totAx))) return rc;
+  if ((rc = devAlloc(&B->db, (size_t)B->pools.totB))) return rc;
+  if ((rc = devAlloc(&B->dx, (size_t)B->pools.totQ))) return rc;
+  if ((rc = devAlloc(&B->ds, (size_t)B->pools.totB))) return rc;
+  if ((rc = devAlloc(&B->dz, (size_t)B->pools.totB))) return rc;
+  if ((rc = devAlloc(&B->dRes, N))) return rc;
+  if ((rc = devAlloc(&B->dWx, (size_t)B->pools.totQ))) return rc;
+  if ((rc = devAlloc(&B->dWs, (size_t)B->pools.totB))) return rc;
+  if ((rc = devAlloc(&B->dWz, (size_t)B->pools.totB))) return rc;
+  if ((rc = devAlloc(&B->dHaveWarm, N))) return rc;
+  if ((rc = devAlloc(&B->dCounters, B->groups.size() + 1))) return rc;
+  if ((rc = devAlloc(&B->dOrder, N))) return rc;
+  CX_CUDA(cudaMemcpy(B->dDesc, B->pools.desc.data(), N * sizeof(InstanceDesc), cudaMemcpyHostToDevice));
+  if (!B->pools.ipool.empty())
+    CX_CUDA(cudaMemcpy(B->dIpool, B->pools.ipool.data(), B->pools.ipool.size() * sizeof(int), cudaMemcpyHostToDevice));
+  if (!B->pools.dpool.empty())
+    CX_CUDA(cudaMemcpy(B->dDpool, B->pools.dpool.data(), B->pools.dpool.size() * sizeof(double), cudaMemcpyHostToDevice));
+  CX_CUDA(cudaMemcpy(B->dOrder, B->order.data(), N * sizeof(int), cudaMemcpyHostToDevice));
+  CX_CUDA(cudaMemset(B->dHaveWarm, 0, N));
+  return CXG_OK;
+}
+
+static std::string checkFinite(const double* v, int64_t n, const char* name) {
+  for (int64_t i = 0; i < n; ++i)
+    if (!std::isfinite(v[i])) return std::string(name) + " contains a non-finite value";
+  return "";
+}
+
+extern "C" int cxg_batch_create(cxg_batch** out, int count, const cxg_problem* problems,
+                                const cxg_settings* settings) {
+  if (!out) return setErr(CXG_E_INVALID, "null output handle");
+  *out = nullptr;
+  if (count < 1 || !problems) return setErr(CXG_E_INVALID, "count must be >= 1");
+  const auto t0 = std::chrono::steady_clock::now();
+  cxg_settings st;
+  if (settings) st = *settings;
+  else {
+    cxg_default_settings(&st);
+    st.precision = CXG_PRECISION_MIXED;
+  }
+  for (int i = 0; i < count; ++i) {
+    std::string e = validateProblem(problems[i]);
+    if (!e.empty()) return setErr(CXG_E_INVALID, "instance " + std::to_string(i) + ": " + e);
+    const cxg_problem& pr = problems[i];
+    e = checkFinite(pr.Px, pr.Pp[pr.n], "P");
+    if (e.empty()) e = checkFinite(pr.Ax, pr.Ap[pr.n], "A");
+    if (e.empty()) e = checkFinite(pr.q, pr.n, "q");
+    if (e.empty()) e = checkFinite(pr.b, pr.m, "b");
+    if (!e.empty()) return setErr(CXG_E_INVALID, "instance " + std::to_string(i) + ": " + e);
+    if (pr.n + pr.zero_dim > 4096)
+      return setErr(CXG_E_UNSUPPORTED, "instance " + std::to_string(i) +
+                                           ": n + zero_dim > 4096 exceeds the single-CTA device path");
+  }
+  cxg_batch* B = new (std::nothrow) cxg_batch();
+  if (!B) return setErr(CXG_E_NOMEM, "host allocation failed");
+  B->count = count;
+  B->st = st;
+  B->kktSt = st;
+  try {
+    for (int i = 0; i < count; ++i) {
+      const cxg_problem& pr = problems[i];
+      planInstance(pr, st, B->pools);
+      B->Pp.emplace_back(pr.Pp, pr.Pp + pr.n + 1);
+      B->Pi.emplace_back(pr.Pi, pr.Pi + pr.Pp[pr.n]);
+      B->Ap.emplace_back(pr.Ap, pr.Ap + pr.n + 1);
+      B->Ai.emplace_back(pr.Ai, pr.Ai + pr.Ap[pr.n]);
+    }
+  } catch (const std::exception& ex) {
+    delete B;
+    return setErr(CXG_E_NOMEM, std::string("planning failed: ") + ex.what());
+  }
+  int rc = CXG_OK;
+  if (cudaStreamCreateWithFlags(&B->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete B;
+    return setErr(CXG_E_CUDA, "cudaStreamCreate failed (no CUDA device?)");
+  }
+  if ((rc = buildGroups(B)) || (rc = uploadPlan(B))) {
+    delete B;
+    return rc;
+  }
+  // initial values
+  std::vector<double> hv;
+  auto upload = [&](double* dst, int64_t total, int which) -> int {
+    hv.assign((size_t)std::max<int64_t>(total, 1), 0.0);
+    for (int i = 0; i < count; ++i) {
+      const cxg_problem& pr = problems[i];
+      const InstanceDesc& D = B->pools.desc[(size_t)i];
+      if (which == 0) std::copy(pr.Px, pr.Px + D.nnzPu, hv.begin() + D.vPx);
+      if (which == 1) std::copy(pr.q, pr.q + D.n, hv.begin() + D.vQ);
+      if (which == 2) std::copy(pr.Ax, pr.Ax + D.nnzA, hv.begin() + D.vAx);
+      if (which == 3) std::copy(pr.b, pr.b + D.m, hv.begin() + D.vB);
+    }
+    if (total > 0) CX_CUDA(cudaMemcpy(dst, hv.data(), (size_t)total * sizeof(double), cudaMemcpyHostToDevice));
+    return CXG_OK;
+  };
+  if ((rc = upload(B->dPx, B->pools.totPx, 0)) || (rc = upload(B->dq, B->pools.totQ, 1)) ||
+      (rc = upload(B->dAx, B->pools.totAx, 2)) || (rc = upload(B->db, B->pools.totB, 3))) {
+    delete B;
+    return rc;
+  }
+  B->hRes.resize((size_t)count);
+  B->setupTime = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  *out = B;
+  return CXG_OK;
+}
+
+extern "C" void cxg_batch_destroy(cxg_batch* b) { delete b; }
+extern "C" int cxg_batch_count(const cxg_batch* b) { return b ? b->count : 0; }
+
+extern "C" int cxg_batch_sizes(const cxg_batch* b, int64_t* nnzP, int64_t* n, int64_t* nnzA, int64_t* m) {
+  if (!b) return setErr(CXG_E_INVALID, "null batch");
+  if (nnzP) *nnzP = b->pools.totPx;
+  if (n) *n = b->pools.totQ;
+  if (nnzA) *nnzA = b->pools.totAx;
+  if (m) *m = b->pools.totB;
+  return CXG_OK;
+}
+
+extern "C" int cxg_batch_offsets(const cxg_batch* b, int i, int64_t* pOff, int64_t* nOff, int64_t* aOff, int64_t* mOff) {
+  if (!b || i < 0 || i >= b->count) return setErr(CXG_E_INVALID, "bad batch or index");
+  const InstanceDesc& D = b->pools.desc[(size_t)i];
+  if (pOff) *pOff = D.vPx;
+  if (nOff) *nOff = D.vQ;
+  if (aOff) *aOff = D.vAx;
+  if (mOff) *mOff = D.vB;
+  return CXG_OK;
+}
+
+static int copyValues(cxg_batch* B, const double* Px, const double* q, const double* Ax, const double* b,
+                      cudaMemcpyKind kind, cudaStream_t s) {
+  if (Px && B->pools.totPx) CX_CUDA(cudaMemcpyAsync(B->dPx, Px, (size_t)B->pools.totPx * 8, kind, s));
+  if (q && B->pools.totQ) CX_CUDA(cudaMemcpyAsync(B->dq, q, (size_t)B->pools.totQ * 8, kind, s));
+  if (Ax && B->pools.totAx) CX_CUDA(cudaMemcpyAsync(B->dAx, Ax, (size_t)B->pools.totAx * 8, kind, s));
+  if (b && B->pools.totB) CX_CUDA(cudaMemcpyAsync(B->db, b, (size_t)B->pools.totB * 8, kind, s));
+  return CXG_OK;
+}
+
+extern "C" int cxg_batch_update_values(cxg_batch* B, const double* Px, const double* q, const double* Ax, const double* b) {
+  if (!B) return setErr(CXG_E_INVALID, "null batch");
+  int rc = copyValues(B, Px, q, Ax, b, cudaMemcpyHostToDevice, B->stream);
+  if (rc) return rc;
+  CX_CUDA(cudaStreamSynchronize(B->stream));
+  return CXG_OK;
+}
+
+extern "C" int cxg_batch_update_values_device(cxg_batch* B, const double* Px, const double* q, const double* Ax,
+                                              const double* b, void* stream) {
+  if (!B) return setErr(CXG_E_INVALID, "null batch");
+  return copyValues(B, Px, q, Ax, b, cudaMemcpyDeviceToDevice, (cudaStream_t)stream);
+}
+
+// Enqueues the device-side solve sequence (queue resets + one persistent launch per group).
+static int enqueueSolve(cxg_batch* B, cudaStream_t s) {
+  const DevSettings ds = makeDevSettings(B->st, B->kktSt);
+  CX_CUDA(cudaMemsetAsync(B->dCounters, 0, sizeof(int) * (B->groups.size() + 1), s));
+  for (const Group& g : B->groups) {
+    LaunchArgs a{};
+    a.desc = B->dDesc;
+    a.order = B->dOrder + g.begin;
+    a.count = g.count;
+    a.counter = B->dCounters + g.counterIdx;
+    a.ipool = B->dIpool;
+    a.dpool = B->dDpool;
+    a.Px = B->dPx;
+    a.q = B->dq;
+    a.Ax = B->dAx;
+    a.b = B->db;
+    a.x = B->dx;
+    a.s = B->ds;
+    a.z = B->dz;
+    a.results = B->dRes;
+    a.warmX = B->dWx;
+    a.warmS = B->dWs;
+    a.warmZ = B->dWz;
+    a.haveWarm = B->dHaveWarm;
+    a.scratch = B->dScratch + g.scratchOff;
+    a.scratchStride = g.stride;
+    a.st = ds;
+    a.lay = g.lay;
+    CX_CUDA(launchIpm(a, g.grid, g.block, g.smem, g.fp32, s));
+  }
+  B->lastLaunches = (int)B->groups.size();
+  return CXG_OK;
+}
+
+// Device-side solve through the captured graph (re-captured when the settings change).
+static int runSolve(cxg_batch* B, cudaStream_t s) {
+  const DevSettings ds = makeDevSettings(B->st, B->kktSt);
+  if (!B->graphValid || !sameDev(ds, B->graphSettings)) {
+    if (B->graphExec) { cudaGraphExecDestroy(B->graphExec); B->graphExec = nullptr; }
+    if (B->graph) { cudaGraphDestroy(B->graph); B->graph = nullptr; }
+    B->graphValid = false;
+    CX_CUDA(cudaStreamBeginCapture(B->stream, cudaStreamCaptureModeThreadLocal));
+    int rc = enqueueSolve(B, B->stream);
+    cudaGraph_t g = nullptr;
+    cudaError_t ce = cudaStreamEndCapture(B->stream, &g);
+    if (rc) { if (g) cudaGraphDestroy(g); return rc; }
+    if (ce != cudaSuccess) return setErr(CXG_E_CUDA, std::string("graph capture: ") + cudaGetErrorString(ce));
+    B->graph = g;
+    CX_CUDA(cudaGraphInstantiate(&B->graphExec, B->graph, 0));
+    B->graphSettings = ds;
+    B->graphValid = true;
+  }
+  CX_CUDA(cudaGraphLaunch(B->graphExec, s));
+  B->lastLaunches = (int)B->groups.size();
+  return CXG_OK;
+}
+
+static double g_clockHz = 0.0;
+
+static void resultToInfo(const DevResult& R, cxg_info& I, double setupTime, double solveTime) {
+  std::memset(&I, 0, sizeof(I));
+  I.status = R.status;
+  I.iterations = R.iterations;
+  I.objective = R.objective;
+  I.primal_residual = R.primal_residual;
+  I.dual_residual = R.dual_residual;
+  I.duality_gap = R.duality_gap;
+  I.mu = R.mu;
+  I.setup_time_s = setupTime;
+  I.solve_time_s = solveTime;
+  I.fp64_fallbacks = R.fp64_fallbacks;
+  I.refine_steps = R.refine_steps;
+  I.max_relres = R.max_relres;
+  if (g_clockHz > 0.0) {
+    I.time_factor_s = (double)R.cycles[1] / g_clockHz;
+    I.time_kkt_solve_s = (double)R.cycles[2] / g_clockHz;
+    I.time_other_s = (double)R.cycles[3] / g_clockHz;
+  }
+}
+
+static int fetchInfo(cxg_batch* B, cxg_info* info, double solveTime) {
+  if (!info) return CXG_OK;
+  if (g_clockHz == 0.0) {
+    int khz = 0;
+    if (cudaDeviceGetAttribute(&khz, cudaDevAttrClockRate, B->device) == cudaSuccess && khz > 0) g_clockHz = khz * 1e3;
+  }
+  CX_CUDA(cudaMemcpy(B->hRes.data(), B->dRes, sizeof(DevResult) * (size_t)B->count, cudaMemcpyDeviceToHost));
+  for (int i = 0; i < B->count; ++i) resultToInfo(B->hRes[(size_t)i], info[i], B->setupTime, solveTime);
+  return CXG_OK;
+}
+
+extern "C" int cxg_batch_solve(cxg_batch* B, double* x, double* s, double* z, cxg_info* info) {
+  if (!B) return setErr(CXG_E_INVALID, "null batch");
+  const auto t0 = std::chrono::steady_clock::now();
+  int rc = runSolve(B, B->stream);
+  if (rc) return rc;
+  if (x && B->pools.totQ) CX_CUDA(cudaMemcpyAsync(x, B->dx, (size_t)B->pools.totQ * 8, cudaMemcpyDeviceToHost, B->stream));
+  if (s && B->pools.totB) CX_CUDA(cudaMemcpyAsync(s, B->ds, (size_t)B->pools.totB * 8, cudaMemcpyDeviceToHost, B->stream));
+  if (z && B->pools.totB) CX_CUDA(cudaMemcpyAsync(z, B->dz, (size_t)B->pools.totB * 8, cudaMemcpyDeviceToHost, B->stream));
+  CX_CUDA(cudaStreamSynchronize(B->stream));
+  const double dt = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  return fetchInfo(B, info, dt);
+}
+
+extern "C" int cxg_batch_solve_device(cxg_batch* B, double* x, double* s, double* z, cxg_info* info, void* stream) {
+  if (!B) return setErr(CXG_E_INVALID, "null batch");
+  cudaStream_t st = (cudaStream_t)stream;
+  int rc = runSolve(B, st);
+  if (rc) return rc;
+  if (x && B->pools.totQ) CX_CUDA(cudaMemcpyAsync(x, B->dx, (size_t)B->pools.totQ * 8, cudaMemcpyDeviceToDevice, st));
+  if (s && B->pools.totB) CX_CUDA(cudaMemcpyAsync(s, B->ds, (size_t)B->pools.totB * 8, cudaMemcpyDeviceToDevice, st));
+  if (z && B->pools.totB) CX_CUDA(cudaMemcpyAsync(z, B->dz, (size_t)B->pools.totB * 8, cudaMemcpyDeviceToDevice, st));
+  if (info) {
+    CX_CUDA(cudaStreamSynchronize(st));
+    return fetchInfo(B, info, 0.0);
+  }
+  return CXG_OK;
+}
+
+extern "C" int cxg_batch_last_launches(const cxg_batch* B) { return B ? B->lastLaunches : 0; }
+
+extern "C" int cxg_batch_footprint(const cxg_batch* B, int64_t* plan, int64_t* values, int64_t* scratch) {
+  if (!B) return setErr(CXG_E_INVALID, "null batch");
+  if (plan)
+    *plan = (int64_t)(B->pools.ipool.size() * sizeof(int) + B->pools.dpool.size() * sizeof(double) +
+                      B->pools.desc.size() * sizeof(InstanceDesc) + B->order.size() * sizeof(int));
+  if (values)
+    *values = 8 * (B->pools.totPx + B->pools.totAx + 2 * B->pools.totQ + 3 * B->pools.totB) +
+              (int64_t)(B->count * sizeof(DevResult));
+  if (scratch) {
+    int64_t t = 0;
+    for (const Group& g : B->groups) t += g.stride * g.grid * 8;
+    *scratch = t;
+  }
+  return CXG_OK;
+}
+
+extern "C" int cxg_batch_describe(const cxg_batch* B, char* buf, int buflen) {
+  if (!B || !buf || buflen <= 0) return setErr(CXG_E_INVALID, "bad arguments");
+  std::string out;
+  for (const Group& g : B->groups) {
+    char line[512];
+    std::snprintf(line, sizeof(line),
+                  "group instances=%d nrMax=%d nMax=%d mMax=%d %s block=%d grid=%d smem=%zu vecInSmem=%d "
+                  "rootInSmem=%d root64InSmem=%d scratchPerCTA=%lld\n",
+                  g.count, g.lay.nrMax, g.lay.nMax, g.lay.mMax, g.fp32 ? "mixed" : "fp64", g.block, g.grid, g.smem,
+                  g.lay.vecInSmem, g.lay.rootInSmem, g.lay.root64InSmem, (long long)g.stride);
+    out += line;
+  }
+  std::snprintf(buf, (size_t)buflen, "%s", out.c_str());
+  return (int)out.size();
+}
+
+// ------------------------------------------------------------------------------------------
+// single instance (conicxx::Solver)
+// ------------------------------------------------------------------------------------------
+struct cxg_solver {
+  cxg_batch* batch = nullptr;
+  cxg_settings st{};
+  bool setupDone = false;
+  int n = 0, m = 0;
+  std::vector<double> d, e;  // equilibration of the setup (host copy for warm-start scaling)
+  double c = 1.0;
+  ~cxg_solver() { delete batch; }
+};
+
+extern "C" int cxg_solver_create(cxg_solver** out) {
+  if (!out) return setErr(CXG_E_INVALID, "null output handle");
+  *out = new (std::nothrow) cxg_solver();
+  if (!*out) return setErr(CXG_E_NOMEM, "host allocation failed");
+  cxg_default_settings(&(*out)->st);
+  return CXG_OK;
+}
+
+extern "C" void cxg_solver_destroy(cxg_solver* s) { delete s; }
+
+extern "C" int cxg_solver_setup(cxg_solver* S, const cxg_problem* pr, const cxg_settings* settings) {
+  if (!S || !pr) return setErr(CXG_E_INVALID, "null argument");
+  S->setupDone = false;
+  delete S->batch;
+  S->batch = nullptr;
+  cxg_settings st;
+  if (settings) st = *settings;
+  else cxg_default_settings(&st);
+  S->st = st;
+  int rc = cxg_batch_create(&S->batch, 1, pr, &st);
+  if (rc) return rc;
+  S->n = pr->n;
+  S->m = pr->m;
+  const InstanceDesc& D = S->batch->pools.desc[0];
+  S->d.assign(S->batch->pools.dpool.begin() + D.dD, S->batch->pools.dpool.begin() + D.dD + D.n);
+  S->e.assign(S->batch->pools.dpool.begin() + D.dE, S->batch->pools.dpool.begin() + D.dE + D.m);
+  S->c = D.cscale;
+  S->setupDone = true;
+  return CXG_OK;
+}
+
+extern "C" int cxg_solver_update_data(cxg_solver* S, const int* Pp, const int* Pi, const double* Px, const double* q,
+                                      const int* Ap, const int* Ai, const double* Ax, const double* b) {
+  if (!S || !S->setupDone) return setErr(CXG_E_NOT_SETUP, "updateData before setup");
+  cxg_batch* B = S->batch;
+  if (Px) {
+    if (!Pp || !Pi) return setErr(CXG_E_INVALID, "P values given without its pattern");
+    if (!samePattern(B->Pp[0], B->Pi[0], S->n, Pp, Pi)) return setErr(CXG_E_PATTERN, "P sparsity pattern changed");
+    std::string e = checkFinite(Px, Pp[S->n], "P");
+    if (!e.empty()) return setErr(CXG_E_INVALID, e);
+  }
+  if (Ax) {
+    if (!Ap || !Ai) return setErr(CXG_E_INVALID, "A values given without its pattern");
+    if (!samePattern(B->Ap[0], B->Ai[0], S->n, Ap, Ai)) return setErr(CXG_E_PATTERN, "A sparsity pattern changed");
+    std::string e = checkFinite(Ax, Ap[S->n], "A");
+    if (!e.empty()) return setErr(CXG_E_INVALID, e);
+  }
+  if (q) { std::string e = checkFinite(q, S->n, "q"); if (!e.empty()) return setErr(CXG_E_INVALID, e); }
+  if (b) { std::string e = checkFinite(b, S->m, "b"); if (!e.empty()) return setErr(CXG_E_INVALID, e); }
+  return cxg_batch_update_values(B, Px, q, Ax, b);
+}
+
+extern "C" int cxg_solver_set_warm_start(cxg_solver* S, const double* x, const double* s, const double* z) {
+  if (!S || !S->setupDone) return CXG_OK;  // the reference silently ignores it before setup
+  if (!x || !s || !z) return setErr(CXG_E_INVALID, "null warm-start vector");
+  cxg_batch* B = S->batch;
+  const bool eq = B->kktSt.equilibrate != 0;
+  std::vector<double> wx(x, x + S->n), ws(s, s + S->m), wz(z, z + S->m);
+  if (eq) {  // equilibration.cpp:135-139
+    for (int i = 0; i < S->n; ++i) wx[(size_t)i] /= S->d[(size_t)i];
+    for (int i = 0; i < S->m; ++i) {
+      wz[(size_t)i] = wz[(size_t)i] * S->c / S->e[(size_t)i];
+      ws[(size_t)i] *= S->e[(size_t)i];
+    }
+  }
+  CX_CUDA(cudaMemcpy(B->dWx, wx.data(), sizeof(double) * wx.size(), cudaMemcpyHostToDevice));
+  if (S->m) {
+    CX_CUDA(cudaMemcpy(B->dWs, ws.data(), sizeof(double) * ws.size(), cudaMemcpyHostToDevice));
+    CX_CUDA(cudaMemcpy(B->dWz, wz.data(), sizeof(double) * wz.size(), cudaMemcpyHostToDevice));
+  }
+  const unsigned char one = 1;
+  CX_CUDA(cudaMemcpy(B->dHaveWarm, &one, 1, cudaMemcpyHostToDevice));
+  return CXG_OK;
+}
+
+extern "C" int cxg_solver_set_settings(cxg_solver* S, const cxg_settings* st) {
+  if (!S || !st) return setErr(CXG_E_INVALID, "null argument");
+  S->st = *st;
+  if (S->batch) S->batch->st = *st;  // KKT fields stay as frozen at setup (kkt_system.cpp:26-31)
+  return CXG_OK;
+}
+
+extern "C" int cxg_solver_get_settings(const cxg_solver* S, cxg_settings* out) {
+  if (!S || !out) return setErr(CXG_E_INVALID, "null argument");
+  *out = S->st;
+  return CXG_OK;
+}
+
+extern "C" int cxg_solver_solve(cxg_solver* S, double* x, double* s, double* z, cxg_info* info) {
+  if (!S) return setErr(CXG_E_INVALID, "null solver");
+  if (!S->setupDone) {  // solver_impl.cpp:369-372 of the reference: NumericalError before setup
+    if (info) {
+      std::memset(info, 0, sizeof(*info));
+      info->status = CXG_STATUS_NUMERICAL_ERROR;
+    }
+    return CXG_OK;
+  }
+  return cxg_batch_solve(S->batch, x, s, z, info);
+}
+
+extern "C" int cxg_solver_backward(cxg_solver* S, const double* dL_dx, double* dq, double* db, double* dPx, double* dAx) {
+  if (!S || !S->setupDone) return setErr(CXG_E_NOT_SETUP, "backward before setup");
+  return cxg_batch_backward(S->batch, dL_dx, dq, db, dPx, dAx);
+}
+
+extern "C" int cxg_batch_backward(cxg_batch* B, const double* dL_dx, double* dq, double* db, double* dPx, double* dAx) {
+  (void)B; (void)dL_dx; (void)dq; (void)db; (void)dPx; (void)dAx;
+  return setErr(CXG_E_UNSUPPORTED, "backward is not built yet");
+}
+
+extern "C" int cxg_batch_backward_device(cxg_batch* B, const double* dL_dx, double* dq, double* db, double* dPx,
+                                         double* dAx, void* stream) {
+  (void)B; (void)dL_dx; (void)dq; (void)db; (void)dPx; (void)dAx; (void)stream;
+  return setErr(CXG_E_UNSUPPORTED, "backward is not built yet");
+}

@@ -1,0 +1,221 @@
+// Device-side cone algebra (FP64), one cone unit per call.
+//
+// Semantics follow src/conicxx/cones/{nonnegative_cone,second_order_cone,zero_cone}.cpp and
+// cone_set.cpp; the Nesterov-Todd scaling of a second-order block is held in eigen-form rather
+// than as the dense W = beta (2 v v' - J) the reference caches (second_order_cone.cpp:132-158):
+// W acts as beta * I off the plane span{e0, (0, u)} (u = v1/|v1|) and as beta * B in it,
+// B = [[2v0^2-1, 2 v0 |v1|], [2 v0 |v1|, 2|v1|^2+1]] with eigenvalues lambda, 1/lambda
+// (det B = 2 v'Jv - 1 = 1). Every operator the interior-point method needs -- W, W^-1,
+// Hs = W^2, Hs + eps I and (Hs + eps I)^-1 -- is then f(W) for a scalar f, applied in O(dim)
+// along the eigenvectors. Applying these near-singular operators as dense matrices loses all
+// accuracy once cond(Hs) approaches 1/eps_machine (Hs * (Hs+eps)^-1 - I reaches O(0.1) in FP64),
+// whereas the eigen-form round trip stays at FP64 rounding.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <math.h>
+
+namespace cxg {
+
+constexpr double kTiny = 1e-12;                    // second_order_cone.cpp:23
+constexpr double kDblMin = 2.2250738585072014e-308;
+constexpr double kStepDegenerateEps = kDblMin * 1e4;  // second_order_cone.cpp:32
+constexpr double kTinyRel = 1e-12;                 // second_order_cone.cpp:89
+constexpr double kAbsFloor = kDblMin * 1e4;        // second_order_cone.cpp:90
+constexpr double kBetaMax = 1e8;                   // second_order_cone.cpp:106
+constexpr double kWMax = 1e8;                      // second_order_cone.cpp:152
+
+// Per-SOC-block scaling parameters (8 doubles in shared memory):
+// [0] kind (0 identity fallback, 1 diagonal, 2 plane), [1] beta, [2] lambda (plane) or
+// a = 2v0^2-1 (diagonal), [3] q1c, [4] q1s (in-plane eigenvector of lambda), [5..7] unused.
+// The unit vector u is kept in a row-indexed array at rows off+1 .. off+dim-1.
+struct SocScale {
+  double kind, beta, lam, qc, qs, r0, r1, r2;
+};
+
+// Computes the NT scaling of one SOC block from (s, z) (second_order_cone.cpp:70-159): the same
+// clamps (margin floors, beta clamp, c floor, v0 floor) and the same identity fallback test on
+// the entries of W = beta (2 v v' - J).
+__device__ __forceinline__ void socUpdateScaling(const double* s, const double* z, int d,
+                                                 SocScale& sc, double* u) {
+  double s1sq = 0, z1sq = 0, sz = 0;
+  for (int i = 1; i < d; ++i) {
+    s1sq += s[i] * s[i];
+    z1sq += z[i] * z[i];
+  }
+  for (int i = 0; i < d; ++i) sz += s[i] * z[i];
+  const double s0 = s[0], z0 = z[0];
+  const double a = sqrt(fmax(fmax(s0 * s0 - s1sq, kTinyRel * s0 * s0), kAbsFloor));
+  const double b = sqrt(fmax(fmax(z0 * z0 - z1sq, kTinyRel * z0 * z0), kAbsFloor));
+  const double beta = fmin(fmax(sqrt(a / b), 1.0 / kBetaMax), kBetaMax);
+  const double c = sqrt(fmax((sz / (a * b) + 1.0) / 2.0, kTiny));
+  // v = (s/a + J z / b) / (2c); v0 += 1; v0 = max(v0, tiny); v /= sqrt(2 v0)
+  const double inv2c = 1.0 / (2.0 * c);
+  double v0 = (z0 / b + s0 / a) / (2.0 * c);
+  v0 += 1.0;
+  v0 = fmax(v0, kTiny);
+  const double nrm = sqrt(2.0 * v0);
+  v0 /= nrm;
+  double n1sq = 0.0, vmax1 = 0.0, vmax2 = 0.0, vdiagmax = 0.0;
+  bool finite = isfinite(v0) && isfinite(beta);
+  for (int i = 1; i < d; ++i) {
+    const double vi = ((-z[i] / b + s[i] / a) / (2.0 * c)) / nrm;
+    (void)inv2c;
+    u[i] = vi;
+    n1sq += vi * vi;
+    const double av = fabs(vi);
+    if (av > vmax1) { vmax2 = vmax1; vmax1 = av; } else if (av > vmax2) { vmax2 = av; }
+    vdiagmax = fmax(vdiagmax, fabs(2.0 * vi * vi + 1.0));
+    finite = finite && isfinite(vi);
+  }
+  // max |W_ij| / beta over the explicit W = beta (2 v v' - J)
+  double wmax = fabs(2.0 * v0 * v0 - 1.0);
+  wmax = fmax(wmax, vdiagmax);
+  wmax = fmax(wmax, 2.0 * fabs(v0) * vmax1);
+  if (d > 2) wmax = fmax(wmax, 2.0 * vmax1 * vmax2);
+  wmax *= beta;
+  // Hs = W W has entries up to ~dim * wmax^2: finite whenever W is finite and wmax <= 1e8.
+  if (!finite || !(wmax <= kWMax)) {
+    sc.kind = 0.0;
+    sc.beta = 1.0;
+    sc.lam = 1.0;
+    sc.qc = 1.0;
+    sc.qs = 0.0;
+    return;
+  }
+  const double n1 = sqrt(n1sq);
+  sc.beta = beta;
+  if (n1 == 0.0 || d == 1) {
+    sc.kind = 1.0;
+    sc.lam = 2.0 * v0 * v0 - 1.0;
+    sc.qc = 1.0;
+    sc.qs = 0.0;
+    for (int i = 1; i < d; ++i) u[i] = 0.0;
+    return;
+  }
+  for (int i = 1; i < d; ++i) u[i] /= n1;
+  const double A = 2.0 * v0 * v0 - 1.0, C = 2.0 * v0 * n1, E = 2.0 * n1 * n1 + 1.0;
+  const double h = 0.5 * (A + E);
+  const double r = hypot(0.5 * (A - E), C);
+  const double l1 = h + r;
+  double qa, qb;
+  if (A >= E) { qa = l1 - E; qb = C; } else { qa = C; qb = l1 - A; }
+  const double qn = hypot(qa, qb);
+  sc.kind = 2.0;
+  sc.lam = l1;
+  sc.qc = qa / qn;
+  sc.qs = qb / qn;
+}
+
+// Scalar functions of W used by the method.
+enum WFun { kW = 0, kWinv = 1, kHs = 2, kHsEps = 3, kGinv = 4 };
+
+__device__ __forceinline__ double wfun(int f, double w, double eps) {
+  switch (f) {
+    case kW: return w;
+    case kWinv: return 1.0 / w;
+    case kHs: return w * w;
+    case kHsEps: return w * w + eps;
+    default: return 1.0 / (w * w + eps);
+  }
+}
+
+// y = f(W) x for one SOC block (x, y may alias only if identical).
+__device__ __forceinline__ void socApply(const SocScale& sc, const double* u, int d, int f, double eps,
+                                         const double* x, double* y) {
+  const int kind = (int)sc.kind;
+  if (kind == 0) {
+    const double g = wfun(f, 1.0, eps);
+    for (int i = 0; i < d; ++i) y[i] = g * x[i];
+    return;
+  }
+  if (kind == 1) {
+    const double g0 = wfun(f, sc.beta * sc.lam, eps), g = wfun(f, sc.beta, eps);
+    const double x0 = x[0];
+    for (int i = 1; i < d; ++i) y[i] = g * x[i];
+    y[0] = g0 * x0;
+    return;
+  }
+  const double x0 = x[0];
+  double xf = 0.0;
+  for (int i = 1; i < d; ++i) xf += u[i] * x[i];
+  const double c1 = sc.qc * x0 + sc.qs * xf;
+  const double c2 = -sc.qs * x0 + sc.qc * xf;
+  const double f1 = wfun(f, sc.beta * sc.lam, eps);
+  const double f2 = wfun(f, sc.beta / sc.lam, eps);
+  const double f3 = wfun(f, sc.beta, eps);
+  const double y0 = f1 * c1 * sc.qc - f2 * c2 * sc.qs;
+  const double yF = f1 * c1 * sc.qs + f2 * c2 * sc.qc;
+  for (int i = 1; i < d; ++i) y[i] = f3 * (x[i] - xf * u[i]) + yF * u[i];
+  y[0] = y0;
+}
+
+// Jordan product (second_order_cone.cpp:43-48); out may alias neither u nor v.
+__device__ __forceinline__ void socProduct(const double* u, const double* v, int d, double* out) {
+  double dt = 0.0;
+  for (int i = 0; i < d; ++i) dt += u[i] * v[i];
+  const double u0 = u[0], v0 = v[0];
+  for (int i = 1; i < d; ++i) out[i] = u0 * v[i] + v0 * u[i];
+  out[0] = dt;
+}
+
+// Inverse Jordan product u \ w (second_order_cone.cpp:50-68).
+__device__ __forceinline__ void socInverseProduct(const double* u, const double* w, int d, double* out) {
+  double u0 = u[0];
+  double u1sq = 0.0, nu = 0.0;
+  for (int i = 1; i < d; ++i) {
+    u1sq += u[i] * u[i];
+    nu += u[i] * w[i];
+  }
+  double rho = u0 * u0 - u1sq;
+  if (fabs(rho) < kTiny) rho = (rho >= 0 ? kTiny : -kTiny);
+  if (fabs(u0) < kTiny) u0 = kTiny;
+  const double w0 = w[0];
+  const double k1 = (nu / u0 - w0), k2 = (rho / u0);
+  for (int i = 1; i < d; ++i) out[i] = (k1 * u[i] + k2 * w[i]) / rho;
+  out[0] = (u0 * w0 - nu) / rho;
+}
+
+// Largest step in [0, amax] keeping x + a dx in the closed SOC (second_order_cone.cpp:174-215).
+__device__ __forceinline__ double socMaxStep(const double* x, const double* dx, int d, double amax) {
+  const double p0 = x[0], d0 = dx[0];
+  double d1sq = 0, p1d1 = 0, p1sq = 0;
+  for (int i = 1; i < d; ++i) {
+    d1sq += dx[i] * dx[i];
+    p1d1 += x[i] * dx[i];
+    p1sq += x[i] * x[i];
+  }
+  const double a = d0 * d0 - d1sq;
+  const double b = 2.0 * (p0 * d0 - p1d1);
+  const double c = p0 * p0 - p1sq;
+  double alpha = amax;
+  if (fabs(a) < kStepDegenerateEps) {
+    if (fabs(b) > kStepDegenerateEps) {
+      const double r = -c / b;
+      if (r > 0 && (p0 + r * d0) >= 0) alpha = fmin(alpha, r);
+    }
+    return alpha;
+  }
+  const double disc = b * b - 4.0 * a * c;
+  if (disc < 0) return alpha;
+  const double sq = sqrt(disc);
+  const double q = (b >= 0) ? -0.5 * (b + sq) : -0.5 * (b - sq);
+  double r1, r2;
+  if (fabs(q) > kStepDegenerateEps) {
+    r1 = q / a;
+    r2 = c / q;
+  } else {
+    r1 = r2 = -b / (2.0 * a);
+  }
+  if (r1 > 0 && (p0 + r1 * d0) >= 0) alpha = fmin(alpha, r1);
+  if (r2 > 0 && (p0 + r2 * d0) >= 0) alpha = fmin(alpha, r2);
+  return alpha;
+}
+
+__device__ __forceinline__ double socMargin(const double* x, int d) {
+  double t = 0.0;
+  for (int i = 1; i < d; ++i) t += x[i] * x[i];
+  return x[0] - sqrt(t);
+}
+
+}  // namespace cxg

@@ -1,0 +1,1187 @@
+// The interior-point hot path on the GPU: one CTA runs the complete homogeneous self-dual
+// embedding IPM of ConicXX (src/conicxx/solver_impl.cpp:220-560 as numbered in that file's
+// SolverImpl::solve and helpers) for one instance at a time, taking instances from an atomic
+// work queue (persistent CTAs, heaviest instances first). All iterates live in shared memory;
+// the problem data is read from HBM/L2.
+//
+// Precision: cone scaling, residuals, refinement residuals, step lengths and termination are
+// FP64. The dense root LDL' (see cxg_layout.h) is FP32 (MIXED) or FP64. In MIXED mode a KKT
+// solve whose FP64-refined relative residual stays above mixed_fallback_tol (or is not finite),
+// or whose FP32 factor has a pivot of the wrong sign, switches that instance to an FP64 factor
+// for the rest of its solve ("sticky" fallback; counted in DevResult::fp64_fallbacks).
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+
+#include "cxg_cones.cuh"
+#include "cxg_kernels.h"
+#include "cxg_layout.h"
+
+namespace cxg {
+
+#define FOR_T(i, n) for (int i = (int)threadIdx.x; i < (n); i += (int)blockDim.x)
+
+// ------------------------------------------------------------------------------------------
+// block reductions (deterministic: fixed summation order, identical result in every thread)
+// ------------------------------------------------------------------------------------------
+template <int K>
+__device__ __forceinline__ void blockSum(double (&v)[K], double* red) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+  for (int k = 0; k < K; ++k)
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_down_sync(0xffffffffu, v[k], o);
+  __syncthreads();
+  if (lane == 0)
+#pragma unroll
+    for (int k = 0; k < K; ++k) red[k * 16 + w] = v[k];
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    double t = 0.0;
+    for (int j = 0; j < nw; ++j) t += red[k * 16 + j];
+    v[k] = t;
+  }
+}
+
+__device__ __forceinline__ double blockMin(double v, double* red) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_down_sync(0xffffffffu, v, o));
+  __syncthreads();
+  if (lane == 0) red[w] = v;
+  __syncthreads();
+  double t = red[0];
+  for (int j = 1; j < nw; ++j) t = fmin(t, red[j]);
+  return t;
+}
+
+__device__ __forceinline__ int blockOrInt(int v, int* redi) {
+  __syncthreads();
+  if (threadIdx.x == 0) redi[0] = 0;
+  __syncthreads();
+  if (v) atomicOr(redi, v);
+  __syncthreads();
+  return redi[0];
+}
+
+// ------------------------------------------------------------------------------------------
+// per-instance context (pointers into shared memory, scratch and the pools)
+// ------------------------------------------------------------------------------------------
+struct Ctx {
+  int n, m, p, l, nsoc, nr, nUnits;
+  const InstanceDesc* D;
+  const int *psRow, *psCol, *pdiag, *plowIdx, *plowSrc, *ap, *ai, *arRow, *arCol, *arSrc;
+  const int *azIdx, *azSrc, *socOff, *socDim, *unitAd, *unitSup, *tgtIdx, *tgtBeg, *contrib;
+  // FP64 scratch (scaled data)
+  double *Pu, *Pv, *Av, *Ad, *T, *qs, *bs, *root64;
+  // shared-memory (or scratch) vectors
+  double *x, *s, *z, *rx, *rz, *x1, *z1, *Px1, *dx, *dz, *ds, *dcon, *lam, *tn, *tm, *tm2;
+  double *rhs, *sol, *res, *cor, *rr, *cw, *cu, *ev;
+  SocScale* sp;
+  void* root;      // FactT root (shared or scratch)
+  double* red;
+  int* redi;
+  double* sc;      // scalar broadcast area
+};
+
+// scalar slots in Ctx::sc
+enum {
+  SC_TAU = 0, SC_KAPPA, SC_EXTRA_P, SC_EXTRA_A, SC_USE64, SC_NFB, SC_RSTEPS, SC_MAXREL,
+  SC_ATTEMPTS, SC_FACTOK, SC_COUNT
+};
+
+// Phase cycle counters (record_timings), kept by thread 0 in the scalar area after PivotStats.
+enum { TM_FACTOR = 0, TM_SOLVE = 1 };
+__device__ __forceinline__ long long* timers(Ctx& c) { return reinterpret_cast<long long*>(c.sc + SC_COUNT + 4); }
+
+// ------------------------------------------------------------------------------------------
+// instance prologue: scaled copies of the data (equilibration.cpp:102-127)
+// ------------------------------------------------------------------------------------------
+__device__ __noinline__ void loadInstance(Ctx& c, const LaunchArgs& a) {
+  const InstanceDesc& D = *c.D;
+  const double* dvec = a.dpool + D.dD;
+  const double* evec = a.dpool + D.dE;
+  const double cs = D.cscale;
+  const double* Px = a.Px + D.vPx;
+  const double* Ax = a.Ax + D.vAx;
+  const double* q = a.q + D.vQ;
+  const double* b = a.b + D.vB;
+  const int* Pp = a.ipool + D.iPp;
+  const int* Pi = a.ipool + D.iPi;
+  const int* psSrc = a.ipool + D.iPsSrc;
+  // scaleP / scaleA / scaleQ / scaleB with the reference's operation order
+  FOR_T(j, c.n) {
+    for (int k = Pp[j]; k < Pp[j + 1]; ++k) c.Pu[k] = Px[k] * (cs * dvec[Pi[k]] * dvec[j]);
+    for (int k = c.ap[j]; k < c.ap[j + 1]; ++k) c.Av[k] = Ax[k] * (evec[c.ai[k]] * dvec[j]);
+    c.qs[j] = q[j] * (cs * dvec[j]);
+  }
+  FOR_T(r, c.m) {
+    c.bs[r] = b[r] * evec[r];
+    c.ev[r] = (r < c.p) ? 0.0 : ((r < c.p + c.l) ? 1.0 : 0.0);
+  }
+  __syncthreads();
+  FOR_T(b2, c.nsoc) c.ev[c.socOff[b2]] = 1.0;
+  FOR_T(k, D.nnzPs) c.Pv[k] = c.Pu[psSrc[k]];
+  const int* adSrc = a.ipool + D.iAdSrc;
+  FOR_T(k, D.nAd) {
+    const int src = adSrc[k];
+    c.Ad[k] = (src >= 0) ? c.Av[src] : 0.0;
+  }
+  __syncthreads();
+}
+
+// ------------------------------------------------------------------------------------------
+// cone-set operations over all units of the instance (cone_set.cpp)
+// ------------------------------------------------------------------------------------------
+__device__ __noinline__ void coneUpdateScaling(Ctx& c, const double* s, const double* z) {
+  FOR_T(t, c.l + c.nsoc) {
+    if (t < c.l) {
+      const int r = c.p + t;
+      c.cw[r] = sqrt(s[r] / z[r]);  // nonnegative_cone.cpp:24
+    } else {
+      const int b = t - c.l;
+      const int off = c.socOff[b], d = c.socDim[b];
+      socUpdateScaling(s + off, z + off, d, c.sp[b], c.cu + off);
+    }
+  }
+  __syncthreads();
+}
+
+// out = f(W) x on every cone row (Zero rows: 0, or eps * x for kHsEps).
+__device__ __noinline__ void coneApply(Ctx& c, int f, double eps, const double* x, double* out) {
+  FOR_T(r, c.p) out[r] = (f == kHsEps) ? eps * x[r] : 0.0;
+  FOR_T(t, c.l + c.nsoc) {
+    if (t < c.l) {
+      const int r = c.p + t;
+      out[r] = wfun(f, c.cw[r], eps) * x[r];
+    } else {
+      const int b = t - c.l;
+      const int off = c.socOff[b], d = c.socDim[b];
+      socApply(c.sp[b], c.cu + off, d, f, eps, x + off, out + off);
+    }
+  }
+  __syncthreads();
+}
+
+// Jordan product / inverse product (Zero rows -> 0).
+__device__ __noinline__ void coneProduct(Ctx& c, bool inverse, const double* u, const double* v, double* out) {
+  FOR_T(r, c.p) out[r] = 0.0;
+  FOR_T(t, c.l + c.nsoc) {
+    if (t < c.l) {
+      const int r = c.p + t;
+      out[r] = inverse ? v[r] / u[r] : u[r] * v[r];
+    } else {
+      const int b = t - c.l;
+      const int off = c.socOff[b], d = c.socDim[b];
+      if (inverse) socInverseProduct(u + off, v + off, d, out + off);
+      else socProduct(u + off, v + off, d, out + off);
+    }
+  }
+  __syncthreads();
+}
+
+// ConeSet::maxStep (cone_set.cpp:108-115) as a block-wide min of per-unit limits.
+__device__ __noinline__ double coneMaxStep(Ctx& c, const double* x, const double* dx, double amax) {
+  double al = amax;
+  FOR_T(t, c.l + c.nsoc) {
+    if (t < c.l) {
+      const int r = c.p + t;
+      if (dx[r] < 0) al = fmin(al, -x[r] / dx[r]);
+    } else {
+      const int b = t - c.l;
+      const int off = c.socOff[b], d = c.socDim[b];
+      al = fmin(al, socMaxStep(x + off, dx + off, d, amax));
+    }
+  }
+  return blockMin(al, c.red);
+}
+
+// ConeSet::margins (cone_set.cpp:77-90): the NN block contributes ONE margin (its minimum).
+__device__ __noinline__ void coneMargins(Ctx& c, const double* x, double& mn, double& pos) {
+  double nnmin = INFINITY;
+  FOR_T(t, c.l) nnmin = fmin(nnmin, x[c.p + t]);
+  double smin = INFINITY, spos = 0.0;
+  FOR_T(b, c.nsoc) {
+    const double mg = socMargin(x + c.socOff[b], c.socDim[b]);
+    smin = fmin(smin, mg);
+    spos += fmax(mg, 0.0);
+  }
+  nnmin = blockMin(nnmin, c.red);
+  smin = blockMin(smin, c.red);
+  double v[1] = {spos};
+  blockSum<1>(v, c.red);
+  mn = fmin(nnmin, smin);
+  pos = v[0] + ((c.l > 0) ? fmax(nnmin, 0.0) : 0.0);
+  if (!isfinite(mn)) mn = 0.0;
+}
+
+__device__ void coneShift(Ctx& c, double* x, double alpha) {
+  FOR_T(t, c.l) x[c.p + t] += alpha;
+  FOR_T(b, c.nsoc) x[c.socOff[b]] += alpha;
+  __syncthreads();
+}
+
+// shiftToInteriorCold (solver_impl.cpp:104-116 in the reference numbering of SolverImpl)
+__device__ void shiftToInteriorCold(Ctx& c, double* v, int degree) {
+  double mn, pos;
+  coneMargins(c, v, mn, pos);
+  const double deg = (double)max(degree, 1);
+  const double target = fmax(1.0, 0.1 * pos / deg);
+  if (mn <= 0.0) {
+    coneShift(c, v, -mn);
+    coneShift(c, v, target);
+  } else if (mn < target) {
+    coneShift(c, v, target - mn);
+  }
+}
+
+__device__ void ensureStrictlyInteriorWarm(Ctx& c, double* v) {
+  double mn, pos;
+  coneMargins(c, v, mn, pos);
+  if (mn <= 1e-8) coneShift(c, v, -mn + 1e-6);
+}
+
+// ------------------------------------------------------------------------------------------
+// SpMVs with the scaled data (FP64)
+// ------------------------------------------------------------------------------------------
+// y = P_sym x (full symmetric CSR, one thread per row)
+__device__ __noinline__ void pmul(Ctx& c, const double* x, double* y) {
+  FOR_T(i, c.n) {
+    double acc = 0.0;
+    for (int k = c.psRow[i]; k < c.psRow[i + 1]; ++k) acc += c.Pv[k] * x[c.psCol[k]];
+    y[i] = acc;
+  }
+  __syncthreads();
+}
+
+// res = rhs - K sol for the statically-regularised K (the matrix refinement targets,
+// kkt_system.cpp:296-311): top = (P + epsP I) x + A'z, bottom = A x - (Hs + epsA I) z.
+__device__ __noinline__ double kktResidual(Ctx& c, const DevSettings& st, const double* rhs, const double* sol,
+                              double* res, double& rhsNorm) {
+  const int n = c.n, m = c.m;
+  const double* xs = sol;
+  const double* zs = sol + n;
+  double acc2[2] = {0.0, 0.0};
+  FOR_T(t, n + m) {
+    if (t < n) {
+      double acc = st.static_reg_P * xs[t];
+      for (int k = c.psRow[t]; k < c.psRow[t + 1]; ++k) acc += c.Pv[k] * xs[c.psCol[k]];
+      for (int k = c.ap[t]; k < c.ap[t + 1]; ++k) acc += c.Av[k] * zs[c.ai[k]];
+      res[t] = rhs[t] - acc;
+    } else {
+      const int r = t - n;
+      double acc = 0.0;
+      for (int k = c.arRow[r]; k < c.arRow[r + 1]; ++k) acc += c.Av[c.arSrc[k]] * xs[c.arCol[k]];
+      res[t] = rhs[t] - acc;
+    }
+  }
+  __syncthreads();
+  // + (Hs + epsA I) z on the cone rows
+  coneApply(c, kHsEps, st.static_reg_A, zs, c.tm2);
+  FOR_T(r, m) res[n + r] += c.tm2[r];
+  __syncthreads();
+  FOR_T(t, n + m) {
+    acc2[0] += res[t] * res[t];
+    acc2[1] += rhs[t] * rhs[t];
+  }
+  blockSum<2>(acc2, c.red);
+  rhsNorm = fmax(sqrt(acc2[1]), 1e-30);
+  return sqrt(acc2[0]) / rhsNorm;
+}
+
+// ------------------------------------------------------------------------------------------
+// dense LDL' of the tiled root (no pivoting) and its solve
+// ------------------------------------------------------------------------------------------
+// Right-looking over 32-wide tile columns J:
+//   (1) one warp factors the diagonal tile (rows in registers, shuffles), stores L (lower),
+//       D (diagonal) and Linv^T (upper half) of the tile;
+//   (2) warps compute the off-diagonal tiles L_IJ = A_IJ Linv_JJ^T D_J^-1;
+//   (3) warps apply the trailing updates A_IK -= L_IJ D_J L_KJ^T, one tile pair per warp.
+// Three barriers per tile column. Pivot rules: QDLDL (qdldl_ldlt.cpp:64-68) fails on an exact
+// zero pivot; REGULARIZED (regularized_ldlt.cpp:132-139, 251-253) corrects a pivot below eps with
+// the expected sign (+ on x rows, - on Zero-cone rows) and fails if > 5% were corrected.
+
+// Pivot statistics written by the factoring warp (shared memory, read after a barrier).
+struct PivotStats {
+  int nreg, zero, wrong, pad;
+  double minAbs;
+};
+
+template <typename T>
+__device__ __forceinline__ T shflT(T v, int src) { return __shfl_sync(0xffffffffu, v, src); }
+
+// Factors diagonal tile J in place (one warp). Global row of tile row r is J*32 + r.
+template <typename T>
+__device__ void tileFactorDiag(T* A, int J, int nr, int nx, const DevSettings& st, PivotStats* ps) {
+  const int r = threadIdx.x & 31;
+  const bool regularized = st.linear_solver == 2;
+  T a[32];
+#pragma unroll
+  for (int col = 0; col < 32; ++col) a[col] = (col <= r) ? A[col * kTileLd + r] : A[r * kTileLd + col];
+  int nreg = 0, zero = 0, wrong = 0;
+  double minAbs = INFINITY;
+#pragma unroll
+  for (int j = 0; j < 32; ++j) {
+    T dj = shflT(a[j], j);
+    const int g = J * 32 + j;
+    if (g < nr) {
+      const double sg = (g < nx) ? 1.0 : -1.0;
+      if (regularized) {
+        double dd = (double)dj;
+        if (dd * sg < st.dynamic_reg_eps) {
+          dd += sg * st.dynamic_reg_delta;
+          if (dd * sg < st.dynamic_reg_eps) dd = sg * st.dynamic_reg_delta;
+          ++nreg;
+          dj = (T)dd;
+        }
+      } else if (dj == (T)0) {
+        zero = 1;
+      }
+      if ((double)dj * sg <= 0.0) wrong = 1;
+      const double ad = fabs((double)dj);
+      minAbs = isfinite(ad) ? fmin(minAbs, ad) : NAN;
+    }
+    const T inv = (T)1 / dj;
+    const T lj = a[j] * inv;
+#pragma unroll
+    for (int k = j + 1; k < 32; ++k) {
+      const T akj = shflT(a[j], k);
+      a[k] -= lj * akj;
+    }
+    if (r > j) a[j] = lj;
+    else if (r == j) a[j] = dj;
+  }
+  __syncwarp();
+#pragma unroll
+  for (int col = 0; col < 32; ++col)
+    if (col <= r) A[col * kTileLd + r] = a[col];
+  __syncwarp();
+  // Linv (unit lower): row r by forward substitution, stored transposed in the upper half
+  T iv[32];
+#pragma unroll
+  for (int col = 0; col < 32; ++col) iv[col] = (col == r) ? (T)1 : (T)0;
+#pragma unroll
+  for (int k = 0; k < 32; ++k) {
+    const T lrk = (r > k) ? A[k * kTileLd + r] : (T)0;
+#pragma unroll
+    for (int col = 0; col <= k; ++col) {
+      const T v = (col == k) ? (T)1 : shflT(iv[col], k);
+      iv[col] -= lrk * v;
+    }
+  }
+#pragma unroll
+  for (int col = 0; col < 32; ++col)
+    if (col < r) A[r * kTileLd + col] = iv[col];
+  // every lane saw the same (shuffled) pivots, so lane 0's statistics are the tile's
+  if (r == 0) {
+    ps->nreg += nreg;
+    ps->zero |= zero;
+    ps->wrong |= wrong;
+    ps->minAbs = (isnan(minAbs) || isnan(ps->minAbs)) ? NAN : fmin(ps->minAbs, minAbs);
+  }
+}
+
+// L_IJ = A_IJ Linv_JJ^T D_J^-1 for one off-diagonal tile (one warp), in place. Column c of the
+// result needs columns k <= c of A only, so the right half (c >= 16) is produced first.
+template <typename T>
+__device__ void tileOffDiag(T* Aij, const T* Ajj) {
+  const int lane = threadIdx.x & 31, lr = lane & 7, lc = lane >> 3;
+#pragma unroll
+  for (int pass = 1; pass >= 0; --pass) {
+    const int c0 = pass * 16 + lc * 4;
+    T acc[4][4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) acc[i][j] = (T)0;
+    for (int k = 0; k < 32; ++k) {
+      T av[4], cv[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) av[i] = Aij[k * kTileLd + lr * 4 + i];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const int col = c0 + j;
+        cv[j] = (k < col) ? Ajj[col * kTileLd + k] : ((k == col) ? (T)1 : (T)0);
+      }
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] += av[i] * cv[j];
+    }
+    __syncwarp();
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int col = c0 + j;
+      const T dinv = (T)1 / Ajj[col * kTileLd + col];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) Aij[col * kTileLd + lr * 4 + i] = acc[i][j] * dinv;
+    }
+    __syncwarp();
+  }
+}
+
+// C -= A diag(d) B^T for 32x32 tiles (one warp); d = diagonal of the factored tile Ajj.
+template <typename T>
+__device__ void tileSyrk(T* C, const T* A, const T* B, const T* Ajj) {
+  const int lane = threadIdx.x & 31, lr = lane & 7, lc = lane >> 3;
+#pragma unroll
+  for (int pass = 0; pass < 2; ++pass) {
+    const int c0 = pass * 16 + lc * 4;
+    T acc[4][4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) acc[i][j] = (T)0;
+    for (int k = 0; k < 32; ++k) {
+      const T dk = Ajj[k * kTileLd + k];
+      T av[4], bv[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) av[i] = A[k * kTileLd + lr * 4 + i];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) bv[j] = B[k * kTileLd + c0 + j] * dk;
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] += av[i] * bv[j];
+    }
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+#pragma unroll
+      for (int i = 0; i < 4; ++i) C[(c0 + j) * kTileLd + lr * 4 + i] -= acc[i][j];
+  }
+}
+
+template <typename T>
+__device__ void denseLdlt(Ctx& c, T* M, const DevSettings& st, int& fail, int& wrongSign, double& minAbsD) {
+  const int nr = c.nr, nx = c.n, Tn = rootTiles(nr);
+  const int warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  PivotStats* ps = reinterpret_cast<PivotStats*>(c.sc + SC_COUNT);
+  if (threadIdx.x == 0) {
+    ps->nreg = 0;
+    ps->zero = 0;
+    ps->wrong = 0;
+    ps->minAbs = INFINITY;
+  }
+  __syncthreads();
+  for (int J = 0; J < Tn; ++J) {
+    T* Ajj = M + tileBase(Tn, J, J);
+    if (warp == 0) tileFactorDiag<T>(Ajj, J, nr, nx, st, ps);
+    __syncthreads();
+    for (int I = J + 1 + warp; I < Tn; I += nw) tileOffDiag<T>(M + tileBase(Tn, I, J), Ajj);
+    __syncthreads();
+    const int rem = Tn - J - 1;
+    const int npairs = rem * (rem + 1) / 2;
+    for (int t = warp; t < npairs; t += nw) {
+      // pair t -> (I, K) with J < K <= I < Tn, enumerated column by column
+      int K = J + 1, tt = t, len = rem;
+      while (tt >= len) { tt -= len; --len; ++K; }
+      const int I = K + tt;
+      tileSyrk<T>(M + tileBase(Tn, I, K), M + tileBase(Tn, I, J), M + tileBase(Tn, K, J), Ajj);
+    }
+    __syncthreads();
+  }
+  const bool regularized = st.linear_solver == 2;
+  fail = regularized ? (((double)ps->nreg > 0.05 * (double)nr) ? 1 : 0) : ps->zero;
+  wrongSign = ps->wrong;
+  minAbsD = ps->minAbs;
+  __syncthreads();
+}
+
+// y <- M^-1 y for the factored tiled root; y has Tn*32 entries (padding entries are zero).
+template <typename T>
+__device__ void denseSolve(Ctx& c, const T* M, T* y) {
+  const int Tn = rootTiles(c.nr);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int nth = blockDim.x;
+  // forward: y_J = Linv_JJ y_J, then y_I -= L_IJ y_J for I > J
+  for (int J = 0; J < Tn; ++J) {
+    const T* Ajj = M + tileBase(Tn, J, J);
+    if (warp == 0) {
+      T acc = y[J * 32 + lane];
+      for (int col = 0; col < lane; ++col) acc += Ajj[lane * kTileLd + col] * y[J * 32 + col];
+      __syncwarp();
+      y[J * 32 + lane] = acc;
+    }
+    __syncthreads();
+    const int rows = (Tn - J - 1) * 32;
+    for (int t = threadIdx.x; t < rows; t += nth) {
+      const int I = J + 1 + t / 32, rr = t % 32;
+      const T* Lij = M + tileBase(Tn, I, J);
+      T acc = (T)0;
+      for (int col = 0; col < 32; ++col) acc += Lij[col * kTileLd + rr] * y[J * 32 + col];
+      y[I * 32 + rr] -= acc;
+    }
+    __syncthreads();
+  }
+  for (int t = threadIdx.x; t < Tn * 32; t += nth) {
+    const int J = t / 32, rr = t % 32;
+    y[t] /= M[tileBase(Tn, J, J) + rr * kTileLd + rr];
+  }
+  __syncthreads();
+  // backward: x_J = Linv_JJ^T y_J, then y_K -= L_JK^T x_J for K < J
+  for (int J = Tn - 1; J >= 0; --J) {
+    const T* Ajj = M + tileBase(Tn, J, J);
+    if (warp == 0) {
+      T acc = y[J * 32 + lane];
+      for (int row = lane + 1; row < 32; ++row) acc += Ajj[row * kTileLd + lane] * y[J * 32 + row];
+      __syncwarp();
+      y[J * 32 + lane] = acc;
+    }
+    __syncthreads();
+    if (J == 0) break;
+    for (int t = threadIdx.x; t < J * 32; t += nth) {
+      const int K = t / 32, cc = t % 32;
+      const T* Ljk = M + tileBase(Tn, J, K);
+      T acc = (T)0;
+      for (int row = 0; row < 32; ++row) acc += Ljk[cc * kTileLd + row] * y[J * 32 + row];
+      y[K * 32 + cc] -= acc;
+    }
+    __syncthreads();
+  }
+}
+
+// ------------------------------------------------------------------------------------------
+// reduced KKT: assembly + factorisation, and one solve through it
+// ------------------------------------------------------------------------------------------
+// Builds the root for the current cone scaling with extra diagonal bumps (ep on x rows, -ea on
+// all cone rows, the regularisation ladder of kkt_system.cpp:152-168) and factors it in T.
+template <typename T>
+__device__ __noinline__ void assembleFactor(Ctx& c, const DevSettings& st, T* M, double ep, double ea,
+                               int& fail, int& wrongSign, double& minAbsD) {
+  const InstanceDesc& D = *c.D;
+  const int n = c.n, nr = c.nr;
+  const double epsA = st.static_reg_A + ea;
+  // T_u = G_u Ad_u with G_u = (Hs_u + epsA I)^-1, column by column
+  FOR_T(u, c.nUnits) {
+    const int a0 = c.unitAd[u], a1 = c.unitAd[u + 1];
+    if (u < c.l) {
+      const double w = c.cw[c.p + u];
+      const double g = 1.0 / (w * w + epsA);
+      for (int k = a0; k < a1; ++k) c.T[k] = g * c.Ad[k];
+    } else {
+      const int b = u - c.l;
+      const int off = c.socOff[b], d = c.socDim[b];
+      for (int k = a0; k < a1; k += d) socApply(c.sp[b], c.cu + off, d, kGinv, epsA, c.Ad + k, c.T + k);
+    }
+  }
+  const int64_t rs = rootSize(nr);
+  for (int64_t t = threadIdx.x; t < rs; t += blockDim.x) M[t] = (T)0;
+  __syncthreads();
+  for (int i = nr + (int)threadIdx.x; i < rootTiles(nr) * kTile; i += blockDim.x) M[rootIdx(nr, i, i)] = (T)1;
+  FOR_T(i, n) {
+    const int src = c.pdiag[i];
+    M[rootIdx(nr, i, i)] = (T)(((src >= 0) ? c.Pu[src] : 0.0) + st.static_reg_P + ep);
+  }
+  FOR_T(k, D.nPlow) M[c.plowIdx[k]] = (T)c.Pu[c.plowSrc[k]];
+  FOR_T(k, D.nAZ) M[c.azIdx[k]] = (T)c.Av[c.azSrc[k]];
+  FOR_T(r, c.p) M[rootIdx(nr, n + r, n + r)] = (T)(-(st.static_reg_A + ea));
+  __syncthreads();
+  FOR_T(t, D.nTgt) {
+    double acc = 0.0;
+    for (int q = c.tgtBeg[t]; q < c.tgtBeg[t + 1]; ++q) {
+      const int oi = c.contrib[3 * q], oj = c.contrib[3 * q + 1], d = c.contrib[3 * q + 2];
+      for (int r = 0; r < d; ++r) acc += c.Ad[oi + r] * c.T[oj + r];
+    }
+    M[c.tgtIdx[t]] += (T)acc;
+  }
+  __syncthreads();
+  denseLdlt<T>(c, M, st, fail, wrongSign, minAbsD);
+}
+
+// sol = Kreg^-1 rhs through the factored root (T) with the bump ea used at factorisation.
+template <typename T>
+__device__ __noinline__ void reducedSolve(Ctx& c, const DevSettings& st, const T* M, double ea,
+                             const double* rhs, double* sol) {
+  const int n = c.n, m = c.m, p = c.p, nr = c.nr;
+  const double epsA = st.static_reg_A + ea;
+  const double* r1 = rhs;
+  const double* r2 = rhs + n;
+  // u = G_C r2_C
+  coneApply(c, kGinv, epsA, r2, c.tm);
+  // t = [r1 + A_C' u ; r2_Z] in T precision
+  T* y = reinterpret_cast<T*>(c.rr);
+  FOR_T(j, n) {
+    double acc = r1[j];
+    for (int k = c.ap[j]; k < c.ap[j + 1]; ++k) {
+      const int r = c.ai[k];
+      if (r >= p) acc += c.Av[k] * c.tm[r];
+    }
+    y[j] = (T)acc;
+  }
+  FOR_T(r, p) y[n + r] = (T)r2[r];
+  for (int i = nr + (int)threadIdx.x; i < rootTiles(nr) * kTile; i += blockDim.x) y[i] = (T)0;
+  __syncthreads();
+  denseSolve<T>(c, M, y);
+  FOR_T(j, n) sol[j] = (double)y[j];
+  FOR_T(r, p) sol[n + r] = (double)y[n + r];
+  __syncthreads();
+  // z_C = G_C (A_C x - r2_C)
+  FOR_T(r, m) {
+    if (r >= p) {
+      double acc = -r2[r];
+      for (int k = c.arRow[r]; k < c.arRow[r + 1]; ++k) acc += c.Av[c.arSrc[k]] * sol[c.arCol[k]];
+      c.tm[r] = acc;
+    }
+  }
+  __syncthreads();
+  FOR_T(t, c.l + c.nsoc) {
+    if (t < c.l) {
+      const int r = p + t;
+      const double w = c.cw[r];
+      sol[n + r] = c.tm[r] / (w * w + epsA);
+    } else {
+      const int b = t - c.l;
+      const int off = c.socOff[b], d = c.socDim[b];
+      socApply(c.sp[b], c.cu + off, d, kGinv, epsA, c.tm + off, sol + n + off);
+    }
+  }
+  __syncthreads();
+  (void)nr;
+}
+
+// Factorisation state of the current iteration.
+struct FactState {
+  int use64;      // factor currently held in FP64 (root64)
+  double ep, ea;  // bumps of the held factor
+};
+
+template <typename FT>
+__device__ __forceinline__ FT* rootT(Ctx& c) { return reinterpret_cast<FT*>(c.root); }
+
+// factorizeWithRetry (kkt_system.cpp:242-264) on the reduced system. In MIXED precision an FP32
+// factor with a wrong-signed pivot is replaced by the FP64 factor (sticky).
+template <typename FT>
+__device__ __noinline__ bool factorizeWithRetryImpl(Ctx& c, const DevSettings& st, FactState& fs) {
+  double ep = 0.0, ea = 0.0;
+  for (int attempt = 0; attempt < 18; ++attempt) {
+    int fail = 0, wrong = 0;
+    double mind = 0.0;
+    if (!fs.use64) {
+      assembleFactor<FT>(c, st, rootT<FT>(c), ep, ea, fail, wrong, mind);
+      if (sizeof(FT) == 4 && (wrong || !isfinite(mind))) {
+        fs.use64 = 1;
+        if (threadIdx.x == 0) c.sc[SC_NFB] += 1.0;
+        attempt -= 1;  // retry this attempt in FP64
+        continue;
+      }
+    } else {
+      assembleFactor<double>(c, st, c.root64, ep, ea, fail, wrong, mind);
+    }
+    if (threadIdx.x == 0) c.sc[SC_ATTEMPTS] += 1.0;
+    if (!fail && isfinite(mind) && mind > st.dynamic_reg_eps) {
+      fs.ep = ep;
+      fs.ea = ea;
+      return true;
+    }
+    ep = fmax(ep * 10.0, st.dynamic_reg_delta);
+    ea = fmax(ea * 10.0, st.dynamic_reg_delta);
+  }
+  return false;
+}
+
+template <typename FT>
+__device__ void solveOnce(Ctx& c, const DevSettings& st, const FactState& fs, const double* rhs, double* sol) {
+  if (fs.use64)
+    reducedSolve<double>(c, st, c.root64, fs.ea, rhs, sol);
+  else
+    reducedSolve<FT>(c, st, rootT<FT>(c), fs.ea, rhs, sol);
+}
+
+__device__ __noinline__ bool vecFinite(Ctx& c, const double* v, int len) {
+  int bad = 0;
+  FOR_T(i, len) if (!isfinite(v[i])) bad = 1;
+  return blockOrInt(bad, c.redi) == 0;
+}
+
+// KktSystem::solve (kkt_system.cpp:296-311) incl. escalateAndResolve (:266-294), plus the
+// MIXED-precision FP64 fallback. Returns the final relative residual.
+template <typename FT>
+__device__ bool factorizeWithRetry(Ctx& c, const DevSettings& st, FactState& fs);
+
+template <typename FT>
+__device__ __noinline__ double kktSolveImpl(Ctx& c, const DevSettings& st, FactState& fs, const double* rhs, double* sol) {
+  const int N = c.n + c.m;
+  for (int pass = 0; pass < 2; ++pass) {
+    solveOnce<FT>(c, st, fs, rhs, sol);
+    if (!vecFinite(c, sol, N)) {
+      // escalate: x1000 bumps from the held factor's, up to 10 times
+      double ep = fs.ep, ea = fs.ea;
+      bool ok = false;
+      for (int att = 0; att < 10 && !ok; ++att) {
+        ep = fmax(ep * 1000.0, st.dynamic_reg_delta);
+        ea = fmax(ea * 1000.0, st.dynamic_reg_delta);
+        int fail = 0, wrong = 0;
+        double mind = 0.0;
+        if (fs.use64)
+          assembleFactor<double>(c, st, c.root64, ep, ea, fail, wrong, mind);
+        else
+          assembleFactor<FT>(c, st, rootT<FT>(c), ep, ea, fail, wrong, mind);
+        if (fail || !isfinite(mind) || !(mind > st.dynamic_reg_eps)) continue;
+        fs.ep = ep;
+        fs.ea = ea;
+        solveOnce<FT>(c, st, fs, rhs, sol);
+        ok = vecFinite(c, sol, N);
+      }
+    }
+    double rhsNorm = 1.0;
+    double rel = kktResidual(c, st, rhs, sol, c.res, rhsNorm);
+    const int maxRef = (sizeof(FT) == 4 && !fs.use64) ? st.mixed_refine_max_iter : st.refine_max_iter;
+    int steps = 0;
+    for (int it = 0; it < maxRef && rel > st.refine_tol; ++it) {
+      solveOnce<FT>(c, st, fs, c.res, c.cor);
+      FOR_T(i, N) sol[i] += c.cor[i];
+      __syncthreads();
+      rel = kktResidual(c, st, rhs, sol, c.res, rhsNorm);
+      ++steps;
+    }
+    if (threadIdx.x == 0) c.sc[SC_RSTEPS] += steps;
+    const bool mixedFp32 = (sizeof(FT) == 4) && !fs.use64;
+    if (mixedFp32 && !(rel <= st.mixed_fallback_tol)) {
+      // sticky FP64 fallback: refactor in FP64 (with the retry ladder) and redo this solve
+      fs.use64 = 1;
+      if (threadIdx.x == 0) c.sc[SC_NFB] += 1.0;
+      if (!factorizeWithRetry<FT>(c, st, fs)) return INFINITY;
+      continue;
+    }
+    if (threadIdx.x == 0) {
+      if (!(rel <= c.sc[SC_MAXREL])) c.sc[SC_MAXREL] = rel;
+    }
+    __syncthreads();
+    return rel;
+  }
+  return INFINITY;
+}
+
+template <typename FT>
+__device__ bool factorizeWithRetry(Ctx& c, const DevSettings& st, FactState& fs) {
+  const long long t0 = st.record_timings ? clock64() : 0;
+  const bool ok = factorizeWithRetryImpl<FT>(c, st, fs);
+  if (st.record_timings && threadIdx.x == 0) timers(c)[TM_FACTOR] += clock64() - t0;
+  return ok;
+}
+
+template <typename FT>
+__device__ double kktSolve(Ctx& c, const DevSettings& st, FactState& fs, const double* rhs, double* sol) {
+  const long long t0 = st.record_timings ? clock64() : 0;
+  // the fallback path inside refactors; its time is counted as solve time
+  const double r = kktSolveImpl<FT>(c, st, fs, rhs, sol);
+  if (st.record_timings && threadIdx.x == 0) timers(c)[TM_SOLVE] += clock64() - t0;
+  return r;
+}
+
+// ------------------------------------------------------------------------------------------
+// the IPM driver for one instance (solver_impl.cpp SolverImpl::solve and helpers)
+// ------------------------------------------------------------------------------------------
+template <typename FT>
+__device__ __noinline__ void solveInstance(Ctx& c, const LaunchArgs& a, int inst) {
+  const DevSettings& st = a.st;
+  const InstanceDesc& D = *c.D;
+  const int n = c.n, m = c.m, N = n + m;
+  const int degree = c.l + c.nsoc;
+  FactState fs{0, 0.0, 0.0};
+  double tau = 1.0, kappa = 1.0;
+  int status = 4;  // MaxIterations
+  int iterations = 0;
+  double dqx = 0, dbz = 0, dsz = 0, dxPx = 0, rtau = 0;
+  if (threadIdx.x < SC_COUNT) c.sc[threadIdx.x] = 0.0;
+  if (threadIdx.x < 2) timers(c)[threadIdx.x] = 0;
+  const long long tStart = clock64();
+  __syncthreads();
+
+  const bool useWarm = st.warm_start && a.haveWarm && a.haveWarm[inst];
+  bool initOk = true;
+  if (useWarm) {
+    FOR_T(j, n) c.x[j] = a.warmX[D.vQ + j];
+    FOR_T(r, m) {
+      c.s[r] = (r < c.p) ? 0.0 : a.warmS[D.vB + r];
+      c.z[r] = a.warmZ[D.vB + r];
+    }
+    __syncthreads();
+    ensureStrictlyInteriorWarm(c, c.s);
+    ensureStrictlyInteriorWarm(c, c.z);
+  } else {
+    // computeInitialPoint: Hs = I scaling of the identity element, 1 or 2 KKT solves
+    coneUpdateScaling(c, c.ev, c.ev);
+    if (!factorizeWithRetry<FT>(c, st, fs)) {
+      initOk = false;
+    } else {
+      if (D.pStoredNnz == 0) {
+        FOR_T(j, n) c.rhs[j] = 0.0;
+        FOR_T(r, m) c.rhs[n + r] = c.bs[r];
+        __syncthreads();
+        kktSolve<FT>(c, st, fs, c.rhs, c.sol);
+        FOR_T(j, n) c.x[j] = c.sol[j];
+        FOR_T(r, m) c.s[r] = -c.sol[n + r];
+        FOR_T(j, n) c.rhs[j] = -c.qs[j];
+        FOR_T(r, m) c.rhs[n + r] = 0.0;
+        __syncthreads();
+        kktSolve<FT>(c, st, fs, c.rhs, c.sol);
+        FOR_T(r, m) c.z[r] = c.sol[n + r];
+      } else {
+        FOR_T(j, n) c.rhs[j] = -c.qs[j];
+        FOR_T(r, m) c.rhs[n + r] = c.bs[r];
+        __syncthreads();
+        kktSolve<FT>(c, st, fs, c.rhs, c.sol);
+        FOR_T(j, n) c.x[j] = c.sol[j];
+        FOR_T(r, m) {
+          c.z[r] = c.sol[n + r];
+          c.s[r] = -c.sol[n + r];
+        }
+      }
+      __syncthreads();
+      FOR_T(r, c.p) c.s[r] = 0.0;
+      __syncthreads();
+      shiftToInteriorCold(c, c.s, degree);
+      shiftToInteriorCold(c, c.z, degree);
+      int bad = 0;
+      FOR_T(j, n) if (!isfinite(c.x[j])) bad = 1;
+      FOR_T(r, m) if (!isfinite(c.s[r]) || !isfinite(c.z[r])) bad = 1;
+      initOk = blockOrInt(bad, c.redi) == 0;
+    }
+  }
+  if (!initOk) status = 5;
+
+  for (int iter = 0; initOk && iter < st.max_iter; ++iter) {
+    iterations = iter + 1;
+    // 1. refactorise for the current scaling
+    coneUpdateScaling(c, c.s, c.z);
+    if (!factorizeWithRetry<FT>(c, st, fs)) { status = 5; break; }
+    // 2. constant solve (-q, b) -> x1, z1; Px1
+    FOR_T(j, n) c.rhs[j] = -c.qs[j];
+    FOR_T(r, m) c.rhs[n + r] = c.bs[r];
+    __syncthreads();
+    kktSolve<FT>(c, st, fs, c.rhs, c.sol);
+    FOR_T(j, n) c.x1[j] = c.sol[j];
+    FOR_T(r, m) c.z1[r] = c.sol[n + r];
+    __syncthreads();
+    if (!vecFinite(c, c.sol, N)) { status = 5; break; }
+    pmul(c, c.x1, c.Px1);
+    // 3. residuals
+    pmul(c, c.x, c.tn);  // Px
+    {
+      double v[6] = {0, 0, 0, 0, 0, 0};
+      FOR_T(t, n + m) {
+        if (t < n) {
+          double atz = 0.0;
+          for (int k = c.ap[t]; k < c.ap[t + 1]; ++k) atz += c.Av[k] * c.z[c.ai[k]];
+          const double r = -atz - c.tn[t] - tau * c.qs[t];
+          c.rx[t] = r;
+          v[0] += r * r;
+          v[2] += c.qs[t] * c.x[t];
+          v[5] += c.x[t] * c.tn[t];
+        } else {
+          const int r = t - n;
+          double ax = 0.0;
+          for (int k = c.arRow[r]; k < c.arRow[r + 1]; ++k) ax += c.Av[c.arSrc[k]] * c.x[c.arCol[k]];
+          const double rr = ax + c.s[r] - tau * c.bs[r];
+          c.rz[r] = rr;
+          v[1] += rr * rr;
+          v[3] += c.bs[r] * c.z[r];
+          v[4] += c.s[r] * c.z[r];
+        }
+      }
+      blockSum<6>(v, c.red);
+      dqx = v[2];
+      dbz = v[3];
+      dsz = v[4];
+      dxPx = v[5];
+      rtau = dqx + dbz + kappa + dxPx / tau;
+      const double mu = (dsz + tau * kappa) / (double)(degree + 1);
+      const double nrx = sqrt(v[0]) / tau, nrz = sqrt(v[1]) / tau;
+      const double pobj = (0.5 * dxPx / tau + dqx) / tau;
+      const double dobj = (-0.5 * dxPx / tau - dbz) / tau;
+      // 4. convergence / infeasibility (solver_impl.cpp checkConvergence / checkInfeasibility)
+      const double gapAbs = fabs(pobj - dobj);
+      const double gapTol = st.tol_gap_abs + st.tol_gap_rel * fmax(fabs(pobj), fabs(dobj));
+      if (nrx < st.tol_feas && nrz < st.tol_feas && gapAbs < gapTol && tau > 1e-6) { status = 1; break; }
+      const double ratio = tau / fmax(kappa, 1e-30);
+      if (ratio <= st.tol_infeas) {
+        double w[2] = {0.0, 0.0};
+        FOR_T(r, m) w[0] += c.z[r] * c.z[r];
+        FOR_T(j, n) w[1] += c.x[j] * c.x[j];
+        blockSum<2>(w, c.red);
+        if (dbz < -st.tol_infeas * fmax(1.0, sqrt(w[0]))) { status = 2; break; }
+        if (dqx < -st.tol_infeas * fmax(1.0, sqrt(w[1]))) { status = 3; break; }
+      }
+      // tau_den is the same for the affine and the combined step (solver_impl.cpp:309-310,
+      // 364-365): kappa/tau - q'x1 - b'z1 + (xi-x1)'P(xi-x1) - x1'Px1, xi = x/tau
+      FOR_T(j, n) c.tn[j] = c.x[j] / tau - c.x1[j];
+      __syncthreads();
+      pmul(c, c.tn, c.dx);
+      double td[4] = {0, 0, 0, 0};
+      FOR_T(j, n) {
+        td[0] += c.qs[j] * c.x1[j];
+        td[2] += c.tn[j] * c.dx[j];
+        td[3] += c.x1[j] * c.Px1[j];
+      }
+      FOR_T(r, m) td[1] += c.bs[r] * c.z1[r];
+      blockSum<4>(td, c.red);
+      const double tauDen = kappa / tau - td[0] - td[1] + td[2] - td[3];
+
+      // 5. affine step: rhs (rx, s - rz)
+      FOR_T(j, n) c.rhs[j] = c.rx[j];
+      FOR_T(r, m) c.rhs[n + r] = c.s[r] - c.rz[r];
+      __syncthreads();
+      kktSolve<FT>(c, st, fs, c.rhs, c.sol);
+      if (!vecFinite(c, c.sol, N)) { status = 5; break; }
+      pmul(c, c.sol, c.tn);  // P xv
+      double tn3[3] = {0, 0, 0};
+      FOR_T(j, n) {
+        tn3[0] += c.qs[j] * c.sol[j];
+        tn3[2] += (c.x[j] / tau) * c.tn[j];
+      }
+      FOR_T(r, m) tn3[1] += c.bs[r] * c.sol[n + r];
+      blockSum<3>(tn3, c.red);
+      const double dkrA = tau * kappa;
+      const double tauNumA = rtau - dkrA / tau + tn3[0] + tn3[1] + 2.0 * tn3[2];
+      if (tauDen == 0.0 || !isfinite(tauNumA) || !isfinite(tauDen)) { status = 5; break; }
+      const double dtauA = tauNumA / tauDen;
+      FOR_T(j, n) c.dx[j] = c.sol[j] + dtauA * c.x1[j];
+      FOR_T(r, m) c.dz[r] = c.sol[n + r] + dtauA * c.z1[r];
+      __syncthreads();
+      coneApply(c, kHs, 0.0, c.dz, c.tm);
+      FOR_T(r, m) c.ds[r] = -(c.tm[r] + c.s[r]);
+      __syncthreads();
+      const double dkappaA = -(dkrA + kappa * dtauA) / tau;
+      {
+        int bad = !isfinite(dtauA) || !isfinite(dkappaA);
+        FOR_T(j, n) if (!isfinite(c.dx[j])) bad = 1;
+        FOR_T(r, m) if (!isfinite(c.dz[r]) || !isfinite(c.ds[r])) bad = 1;
+        if (blockOrInt(bad, c.redi)) { status = 5; break; }
+      }
+      // 6. affine step length (no fraction), mu_aff, sigma
+      double aaff = 1.0;
+      if (dtauA < 0) aaff = fmin(aaff, -tau / dtauA);
+      if (dkappaA < 0) aaff = fmin(aaff, -kappa / dkappaA);
+      aaff = coneMaxStep(c, c.z, c.dz, aaff);
+      aaff = coneMaxStep(c, c.s, c.ds, aaff);
+      double sa[1] = {0.0};
+      FOR_T(r, m) sa[0] += (c.s[r] + aaff * c.ds[r]) * (c.z[r] + aaff * c.dz[r]);
+      blockSum<1>(sa, c.red);
+      const double tauAff = tau + aaff * dtauA, kappaAff = kappa + aaff * dkappaA;
+      const double muAff = (sa[0] + tauAff * kappaAff) / (double)(degree + 1);
+      double sigma;
+      if (mu > 0) {
+        const double rt = fmax(muAff / mu, 0.0);
+        sigma = fmin(fmax(rt * rt * rt, 0.0), 1.0);
+      } else {
+        sigma = 1.0;
+      }
+      // 7. combined step: lambda = W z; ds_comb = lambda o lambda + (W^-1 ds_aff) o (W dz_aff) - sigma mu e
+      coneApply(c, kW, 0.0, c.z, c.lam);
+      coneProduct(c, false, c.lam, c.lam, c.tm);           // lambda o lambda
+      coneApply(c, kWinv, 0.0, c.ds, c.tm2);               // W^-1 ds_aff
+      coneApply(c, kW, 0.0, c.dz, c.dcon);                 // W dz_aff (dcon as temp)
+      coneProduct(c, false, c.tm2, c.dcon, c.rhs);         // corrector (rhs as temp, length m)
+      FOR_T(r, m) c.tm2[r] = c.tm[r] + c.rhs[r] - sigma * mu * c.ev[r];
+      __syncthreads();
+      coneProduct(c, true, c.lam, c.tm2, c.tm);            // lambda \ ds_comb
+      coneApply(c, kW, 0.0, c.tm, c.dcon);                 // ds_const = W (lambda \ ds_comb)
+      FOR_T(j, n) c.rhs[j] = (1.0 - sigma) * c.rx[j];
+      FOR_T(r, m) c.rhs[n + r] = c.dcon[r] - (1.0 - sigma) * c.rz[r];
+      __syncthreads();
+      kktSolve<FT>(c, st, fs, c.rhs, c.sol);
+      if (!vecFinite(c, c.sol, N)) { status = 5; break; }
+      pmul(c, c.sol, c.tn);
+      tn3[0] = tn3[1] = tn3[2] = 0.0;
+      FOR_T(j, n) {
+        tn3[0] += c.qs[j] * c.sol[j];
+        tn3[2] += (c.x[j] / tau) * c.tn[j];
+      }
+      FOR_T(r, m) tn3[1] += c.bs[r] * c.sol[n + r];
+      blockSum<3>(tn3, c.red);
+      const double dtrC = (1.0 - sigma) * rtau;
+      const double dkrC = tau * kappa + dtauA * dkappaA - sigma * mu;
+      const double tauNumC = dtrC - dkrC / tau + tn3[0] + tn3[1] + 2.0 * tn3[2];
+      if (tauDen == 0.0 || !isfinite(tauNumC)) { status = 5; break; }
+      const double dtau = tauNumC / tauDen;
+      FOR_T(j, n) c.dx[j] = c.sol[j] + dtau * c.x1[j];
+      FOR_T(r, m) c.dz[r] = c.sol[n + r] + dtau * c.z1[r];
+      __syncthreads();
+      coneApply(c, kHs, 0.0, c.dz, c.tm);
+      FOR_T(r, m) c.ds[r] = -(c.tm[r] + c.dcon[r]);
+      __syncthreads();
+      const double dkappa = -(dkrC + kappa * dtau) / tau;
+      {
+        int bad = !isfinite(dtau) || !isfinite(dkappa);
+        FOR_T(j, n) if (!isfinite(c.dx[j])) bad = 1;
+        FOR_T(r, m) if (!isfinite(c.dz[r]) || !isfinite(c.ds[r])) bad = 1;
+        if (blockOrInt(bad, c.redi)) { status = 5; break; }
+      }
+      // 8. step length with the fraction-to-boundary factor
+      double alpha = 1.0;
+      if (dtau < 0) alpha = fmin(alpha, -tau / dtau);
+      if (dkappa < 0) alpha = fmin(alpha, -kappa / dkappa);
+      alpha = coneMaxStep(c, c.z, c.dz, alpha);
+      alpha = coneMaxStep(c, c.s, c.ds, alpha);
+      alpha *= st.max_step_fraction;
+      if (!isfinite(alpha) || alpha <= 0.0) { status = 5; break; }
+      // 9. update and rescale
+      FOR_T(j, n) c.x[j] += alpha * c.dx[j];
+      FOR_T(r, m) {
+        c.s[r] += alpha * c.ds[r];
+        c.z[r] += alpha * c.dz[r];
+      }
+      tau += alpha * dtau;
+      kappa += alpha * dkappa;
+      __syncthreads();
+      const double scl = fmax(tau, kappa);
+      if (scl > 1e8 || scl < 1e-8) {
+        const double inv = 1.0 / scl;
+        FOR_T(j, n) c.x[j] *= inv;
+        FOR_T(r, m) {
+          c.s[r] *= inv;
+          c.z[r] *= inv;
+        }
+        tau *= inv;
+        kappa *= inv;
+        __syncthreads();
+      }
+    }
+  }
+
+  // finalizeSolution (solver_impl.cpp:342-365 of the reference numbering)
+  const bool infeas = (status == 2 || status == 3);
+  const double scale = infeas ? 1.0 / fmax(kappa, 1e-30) : 1.0 / fmax(tau, 1e-30);
+  const double* dvec = a.dpool + D.dD;
+  const double* evec = a.dpool + D.dE;
+  const double cs = D.cscale;
+  const bool eq = st.equilibrate != 0;
+  FOR_T(j, n) a.x[D.vX + j] = c.x[j] * scale * (eq ? dvec[j] : 1.0);
+  FOR_T(r, m) {
+    a.s[D.vS + r] = eq ? (c.s[r] * scale) / evec[r] : c.s[r] * scale;
+    a.z[D.vZ + r] = eq ? (c.z[r] * scale) * evec[r] / cs : c.z[r] * scale;
+  }
+  double nr2[2] = {0.0, 0.0};
+  FOR_T(j, n) nr2[0] += c.rx[j] * c.rx[j];
+  FOR_T(r, m) nr2[1] += c.rz[r] * c.rz[r];
+  blockSum<2>(nr2, c.red);
+  if (status == 1 && st.warm_start && a.warmX) {
+    FOR_T(j, n) a.warmX[D.vQ + j] = c.x[j];
+    FOR_T(r, m) {
+      a.warmS[D.vB + r] = c.s[r];
+      a.warmZ[D.vB + r] = c.z[r];
+    }
+    if (threadIdx.x == 0 && a.haveWarm) a.haveWarm[inst] = 1;
+  }
+  if (threadIdx.x == 0) {
+    DevResult R{};
+    R.status = status;
+    R.iterations = iterations;
+    double pobj = (0.5 * dxPx / tau + dqx) / tau;
+    double gap = dsz / (tau * tau);
+    if (eq) {
+      pobj /= cs;
+      gap /= cs;
+    }
+    R.objective = pobj;
+    R.duality_gap = gap;
+    R.primal_residual = sqrt(nr2[1]) / fmax(tau, 1e-30);
+    R.dual_residual = sqrt(nr2[0]) / fmax(tau, 1e-30);
+    R.mu = (dsz + tau * kappa) / (double)(degree + 1);
+    R.max_relres = c.sc[SC_MAXREL];
+    R.fp64_fallbacks = (int)c.sc[SC_NFB];
+    R.refine_steps = (int)c.sc[SC_RSTEPS];
+    R.factor_attempts = (int)c.sc[SC_ATTEMPTS];
+    R.error_code = 0;
+    const long long tot = clock64() - tStart;
+    R.cycles[0] = tot;
+    R.cycles[1] = timers(c)[TM_FACTOR];
+    R.cycles[2] = timers(c)[TM_SOLVE];
+    R.cycles[3] = tot - R.cycles[1] - R.cycles[2];
+    a.results[inst] = R;
+  }
+  __syncthreads();
+}
+
+// ------------------------------------------------------------------------------------------
+// kernel: persistent CTAs over an atomic instance queue
+// ------------------------------------------------------------------------------------------
+template <typename FT>
+__global__ void __launch_bounds__(512) ipmKernel(LaunchArgs a) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ int sInst;
+  __shared__ int sRedi[4];
+  __shared__ Ctx c;
+  double* scratch = a.scratch + (int64_t)blockIdx.x * a.scratchStride;
+  const SmemLayout& L = a.lay;
+  for (;;) {
+    if (threadIdx.x == 0) sInst = atomicAdd(a.counter, 1);
+    __syncthreads();
+    const int slot = sInst;
+    __syncthreads();
+    if (slot >= a.count) break;
+    const int inst = a.order[slot];
+    if (threadIdx.x == 0) {
+    const InstanceDesc& D = a.desc[inst];
+    c.D = &D;
+    c.n = D.n; c.m = D.m; c.p = D.p; c.l = D.l; c.nsoc = D.nsoc; c.nr = D.nr; c.nUnits = D.nUnits;
+    const int* I = a.ipool;
+    c.psRow = I + D.iPsRow; c.psCol = I + D.iPsCol; c.pdiag = I + D.iPdiag;
+    c.plowIdx = I + D.iPlowIdx; c.plowSrc = I + D.iPlowSrc;
+    c.ap = I + D.iAp; c.ai = I + D.iAi;
+    c.arRow = I + D.iArRow; c.arCol = I + D.iArCol; c.arSrc = I + D.iArSrc;
+    c.azIdx = I + D.iAZIdx; c.azSrc = I + D.iAZSrc;
+    c.socOff = I + D.iSocOff; c.socDim = I + D.iSocDim;
+    c.unitAd = I + D.iUnitAd; c.unitSup = I + D.iUnitSup;
+    c.tgtIdx = I + D.iTgtIdx; c.tgtBeg = I + D.iTgtBeg; c.contrib = I + D.iContrib;
+    // scratch carve-up for this instance
+    c.Pu = scratch + D.sPv;  // Pu then Pv share the region start (see host layout)
+    c.Pv = c.Pu + D.nnzPu;
+    c.Av = scratch + D.sAv;
+    c.Ad = scratch + D.sAd;
+    c.T = scratch + D.sT;
+    c.qs = scratch + D.sQ;
+    c.bs = scratch + D.sB;
+    c.root64 = L.root64InSmem ? reinterpret_cast<double*>(smem + L.rootOff) : scratch + D.sRoot64;
+    // vectors: shared memory or scratch
+    double* vb = L.vecInSmem ? reinterpret_cast<double*>(smem + L.vecOff) : scratch + D.sVec;
+    const int nM = L.nMax, mM = L.mMax, NM = L.nMax + L.mMax, rM = rootTiles(L.nrMax) * kTile;
+    double* q = vb;
+    auto take = [&](int len) { double* r = q; q += (len + 1) & ~1; return r; };
+    c.x = take(nM); c.rx = take(nM); c.x1 = take(nM); c.Px1 = take(nM); c.dx = take(nM); c.tn = take(nM);
+    c.s = take(mM); c.z = take(mM); c.rz = take(mM); c.z1 = take(mM); c.dz = take(mM); c.ds = take(mM);
+    c.dcon = take(mM); c.lam = take(mM); c.tm = take(mM); c.tm2 = take(mM); c.cw = take(mM); c.cu = take(mM); c.ev = take(mM);
+    c.rhs = take(NM); c.sol = take(NM); c.res = take(NM); c.cor = take(NM);
+    c.rr = take(rM);
+    c.sp = reinterpret_cast<SocScale*>(take(8 * L.nsocMax));
+    (void)take(rM);  // spare root-length vector (kept for the layout count)
+    c.root = L.rootInSmem ? reinterpret_cast<void*>(smem + L.rootOff) : reinterpret_cast<void*>(c.root64);
+    c.red = reinterpret_cast<double*>(smem + L.redOff);
+    c.sc = c.red + 128;
+    c.redi = sRedi;
+    }
+    __syncthreads();
+    loadInstance(c, a);
+    solveInstance<FT>(c, a, inst);
+  }
+}
+
+// explicit instantiations through the host launchers
+cudaError_t launchIpm(const LaunchArgs& a, int grid, int block, size_t smem, bool fp32, cudaStream_t stream) {
+  if (fp32) {
+    cudaError_t e = cudaFuncSetAttribute(ipmKernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    ipmKernel<float><<<grid, block, smem, stream>>>(a);
+  } else {
+    cudaError_t e = cudaFuncSetAttribute(ipmKernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    ipmKernel<double><<<grid, block, smem, stream>>>(a);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t ipmOccupancy(int* blocksPerSM, int block, size_t smem, bool fp32) {
+  cudaError_t e;
+  if (fp32) {
+    e = cudaFuncSetAttribute(ipmKernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocksPerSM, ipmKernel<float>, block, smem);
+  }
+  e = cudaFuncSetAttribute(ipmKernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocksPerSM, ipmKernel<double>, block, smem);
+}
+
+}  // namespace cxg

@@ -1,0 +1,55 @@
+// Launch interface of the device kernels (cxg_ipm.cu, cxg_adjoint.cu) as seen by the host API.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "cxg_layout.h"
+
+namespace cxg {
+
+// Dynamic shared-memory layout of one launch (byte offsets), sized for the largest instance of
+// the launch. Vectors go to shared memory when they fit, else to the CTA's scratch.
+struct SmemLayout {
+  int nMax, mMax, nrMax, nsocMax;
+  int vecInSmem, rootInSmem, root64InSmem, pad;
+  int64_t redOff, vecOff, rootOff, total;
+};
+
+// Doubles of FP64 vectors per CTA for given maxima (must match the carve-up in ipmKernel).
+inline int64_t vecDoubles(int nMax, int mMax, int nrMax, int nsocMax) {
+  auto r2 = [](int64_t v) { return (v + 1) & ~int64_t(1); };
+  return 6 * r2(nMax) + 13 * r2(mMax) + 4 * r2((int64_t)nMax + mMax) + 2 * (int64_t)rootTiles(nrMax) * kTile +
+         r2(8 * (int64_t)nsocMax);
+}
+
+struct LaunchArgs {
+  const InstanceDesc* desc;
+  const int* order;       // instances of this launch, heaviest first
+  int count;
+  int* counter;           // zeroed before the launch
+  const int* ipool;
+  const double* dpool;
+  const double* Px;       // concatenated user values
+  const double* q;
+  const double* Ax;
+  const double* b;
+  double* x;              // concatenated outputs (user units)
+  double* s;
+  double* z;
+  DevResult* results;
+  double* warmX;          // device-resident warm start (equilibrated space), may be null
+  double* warmS;
+  double* warmZ;
+  unsigned char* haveWarm;
+  double* scratch;        // gridDim.x * scratchStride doubles
+  int64_t scratchStride;
+  DevSettings st;
+  SmemLayout lay;
+};
+
+cudaError_t launchIpm(const LaunchArgs& a, int grid, int block, size_t smem, bool fp32, cudaStream_t stream);
+// Resident CTAs per SM of the IPM kernel for a block size and dynamic shared-memory size.
+cudaError_t ipmOccupancy(int* blocksPerSM, int block, size_t smem, bool fp32);
+
+}  // namespace cxg

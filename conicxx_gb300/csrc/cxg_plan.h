@@ -1,0 +1,38 @@
+// Host-side symbolic set-up of one instance: validation, equilibration, and the device plan
+// (index arrays that stay fixed while only values change, the role SparsityMap + KktSystem::setup
+// play in the reference: src/conicxx/kkt/sparsity_map.cpp:8-56, kkt_system.cpp:22-117).
+#pragma once
+
+#include <string>
+#include <vector>
+
+#include "conicxx_gb300.h"
+#include "cxg_layout.h"
+
+namespace cxg {
+
+struct Pools {
+  std::vector<int> ipool;
+  std::vector<double> dpool;
+  std::vector<InstanceDesc> desc;
+  int64_t totPx = 0, totQ = 0, totAx = 0, totB = 0;  // lengths of the concatenated value arrays
+};
+
+// Structural validation of one problem (cone spec as ConeSpec::isValid, cone_spec.h:25-31,
+// dimensions as SolverImpl::setup, solver_impl.cpp:11-16, plus CSC well-formedness, which the
+// device path needs to index safely). Returns an empty string when valid.
+std::string validateProblem(const cxg_problem& pr);
+
+// Ruiz equilibration (src/conicxx/kkt/equilibration.cpp:8-100) of the RAW data.
+void computeEquilibration(const cxg_problem& pr, const cxg_settings& st, std::vector<double>& d,
+                          std::vector<double>& e, double& c);
+
+// Appends the plan of `pr` to `pools` (values are NOT copied; see packValues).
+void planInstance(const cxg_problem& pr, const cxg_settings& st, Pools& pools);
+
+// Whether P's upper-CSC pattern / A's CSC pattern equal the instance's (updateData check,
+// kkt_system.cpp:10-19).
+bool samePattern(const std::vector<int>& p_ref, const std::vector<int>& i_ref, int cols,
+                 const int* p, const int* i);
+
+}  // namespace cxg

@@ -1,0 +1,221 @@
+/*
+ * conicxx_gb300.h -- C-ABI of the GB300-native ConicXX interior-point path.
+ *
+ * Problem (identical to ConicXX, README.md:21-33):
+ *     minimise    1/2 x'Px + q'x
+ *     subject to  Ax + s = b,   s in K = Zero^p x R^l_+ x Q^k1 x ... x Q^kN
+ *
+ * Every entry point takes plain pointers and sizes; no C++ or torch type crosses this
+ * boundary. Matrices are CSC with 32-bit indices (ConicXX's SparseMat, include/conicxx/types.h:18).
+ * P is given as its upper triangle (entries below the diagonal are ignored, as in
+ * src/conicxx/kkt/kkt_system.cpp:58-65 and the selfadjointView<Upper> product at
+ * src/conicxx/solver_impl.cpp:102).
+ *
+ * Return codes: CXG_OK (0) on success, a negative CXG_E_* on a usage or runtime error.
+ * The solver status of a solve is reported in cxg_info.status (never as a return code).
+ * After any non-zero return, cxg_last_error() gives a message for the calling thread.
+ * No C++ exception ever crosses this boundary.
+ */
+#ifndef CONICXX_GB300_H
+#define CONICXX_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- return codes ------------------------------------------------------------------------ */
+enum {
+  CXG_OK = 0,
+  CXG_E_INVALID = -1,      /* bad argument, dimension mismatch, invalid cone spec */
+  CXG_E_PATTERN = -2,      /* updateData: sparsity pattern differs from setup() */
+  CXG_E_NOT_SETUP = -3,    /* handle used before a successful setup */
+  CXG_E_CUDA = -4,         /* CUDA runtime error (message in cxg_last_error) */
+  CXG_E_NOMEM = -5,        /* host or device allocation failed */
+  CXG_E_UNSUPPORTED = -6,  /* instance too large for the device path, or feature not built */
+  CXG_E_INTERNAL = -7
+};
+
+/* ---- solver status: same values and meaning as conicxx::Status
+ *      (include/conicxx/solution.h:9-16) -------------------------------------------------- */
+enum {
+  CXG_STATUS_UNSOLVED = 0,
+  CXG_STATUS_SOLVED = 1,
+  CXG_STATUS_PRIMAL_INFEASIBLE = 2,
+  CXG_STATUS_DUAL_INFEASIBLE = 3,
+  CXG_STATUS_MAX_ITERATIONS = 4,
+  CXG_STATUS_NUMERICAL_ERROR = 5
+};
+
+/* conicxx::LinearSolverBackend (include/conicxx/settings.h:8-18). The device path has one
+ * factorisation; the value selects its pivot rule: QDLDL = retry ladder only,
+ * REGULARIZED = per-pivot correction plus the ladder. EIGEN behaves as QDLDL. */
+enum { CXG_LINSOLVER_EIGEN = 0, CXG_LINSOLVER_QDLDL = 1, CXG_LINSOLVER_REGULARIZED = 2 };
+
+/* Arithmetic of the KKT factorisation and triangular solves (new; no reference counterpart).
+ * Residuals, refinement residuals, cone scaling, step lengths and termination are FP64 in
+ * both modes. */
+enum { CXG_PRECISION_FP64 = 0, CXG_PRECISION_MIXED = 1 };
+
+/* Field-for-field the reference's Settings (include/conicxx/settings.h:21-62), same defaults
+ * (cxg_default_settings), followed by the GB300 additions. */
+typedef struct cxg_settings {
+  double tol_feas;            /* 1e-8 */
+  double tol_gap_abs;         /* 1e-8 */
+  double tol_gap_rel;         /* 1e-8 */
+  double tol_infeas;          /* 1e-7 */
+  int max_iter;               /* 200 */
+  double static_reg_P;        /* 1e-8 */
+  double static_reg_A;        /* 1e-8 */
+  double dynamic_reg_eps;     /* 1e-14 */
+  double dynamic_reg_delta;   /* 1e-7 */
+  int refine_max_iter;        /* 3 */
+  double refine_tol;          /* 1e-12 */
+  double max_step_fraction;   /* 0.99 */
+  int equilibrate;            /* 1 */
+  int equilibrate_max_iter;   /* 10 */
+  double equilibrate_min_scale; /* 1e-4 */
+  double equilibrate_max_scale; /* 1e4 */
+  int warm_start;             /* 1 */
+  int verbose;                /* 0 (declared, unused, as in the reference) */
+  int record_timings;         /* 0 */
+  int validate_inputs;        /* 1 */
+  int linear_solver;          /* CXG_LINSOLVER_QDLDL */
+  /* ---- GB300 additions ---- */
+  int precision;              /* CXG_PRECISION_FP64 for cxg_solver, MIXED for cxg_batch */
+  int mixed_refine_max_iter;  /* refinement steps allowed on an FP32 factor before the FP64
+                                 refactorisation fallback (default 6) */
+  double mixed_fallback_tol;  /* relative KKT residual above which an FP32-factor solve is redone
+                                 with an FP64 factor (default 1e-10) */
+  int threads_per_instance;   /* 0 = autotuned; else 64/128/256/512 */
+} cxg_settings;
+
+/* conicxx::Info (include/conicxx/solution.h:18-26) plus Solution::objective/status and counters. */
+typedef struct cxg_info {
+  int status;                 /* CXG_STATUS_* */
+  int iterations;
+  double objective;
+  double primal_residual;
+  double dual_residual;
+  double duality_gap;
+  double mu;
+  double setup_time_s;
+  double solve_time_s;
+  int fp64_fallbacks;         /* KKT solves redone with an FP64 factor (mixed precision) */
+  int refine_steps;           /* total refinement steps taken */
+  double max_relres;          /* worst final relative KKT residual over all solves */
+  /* with settings.record_timings: device time split of this instance's solve, seconds */
+  double time_factor_s;       /* KKT assembly + LDL' factorisations */
+  double time_kkt_solve_s;    /* KKT solves incl. iterative refinement */
+  double time_other_s;        /* residuals, cone algebra, step lengths */
+} cxg_info;
+
+/* One problem instance; all pointers are caller-owned host memory (copied, never retained). */
+typedef struct cxg_problem {
+  int n, m;
+  const int* Pp; const int* Pi; const double* Px;   /* n x n, upper triangle, CSC */
+  const double* q;                                  /* n */
+  const int* Ap; const int* Ai; const double* Ax;   /* m x n, CSC */
+  const double* b;                                  /* m */
+  int zero_dim, nonneg_dim, n_soc;                  /* ConeSpec (include/conicxx/cone_spec.h) */
+  const int* soc_dims;
+} cxg_problem;
+
+void cxg_default_settings(cxg_settings* settings);
+const char* cxg_status_string(int status);
+const char* cxg_version(void);
+const char* cxg_last_error(void);
+/* Number of CUDA devices visible to the library (0 without a GPU). Never fails. */
+int cxg_device_count(void);
+
+/* ---- single instance: replaces conicxx::Solver (include/conicxx/solver.h:33-95) ---------- */
+typedef struct cxg_solver cxg_solver;
+
+/* Solver::Solver() (include/conicxx/solver.h:35). */
+int cxg_solver_create(cxg_solver** out);
+void cxg_solver_destroy(cxg_solver* solver);
+/* Solver::setup(P, q, A, b, cone_spec, settings) (include/conicxx/solver.h:46-47). settings may
+ * be NULL (defaults). Returns CXG_E_INVALID where the reference returns false. */
+int cxg_solver_setup(cxg_solver* solver, const cxg_problem* problem, const cxg_settings* settings);
+/* Solver::updateData(P*, q*, A*, b*) (include/conicxx/solver.h:78). Any pointer may be NULL
+ * (unchanged). A matrix is passed as its CSC arrays; CXG_E_PATTERN where the reference returns
+ * false because the pattern changed. */
+int cxg_solver_update_data(cxg_solver* solver, const int* Pp, const int* Pi, const double* Px,
+                           const double* q, const int* Ap, const int* Ai, const double* Ax,
+                           const double* b);
+/* Solver::setWarmStart(x, s, z) (include/conicxx/solver.h:82). */
+int cxg_solver_set_warm_start(cxg_solver* solver, const double* x, const double* s, const double* z);
+/* Solver::setSettings / settings() (include/conicxx/solver.h:84-85). */
+int cxg_solver_set_settings(cxg_solver* solver, const cxg_settings* settings);
+int cxg_solver_get_settings(const cxg_solver* solver, cxg_settings* out);
+/* Solver::solve() + Solution (include/conicxx/solver.h:90, solution.h:28-39). x (n), s (m),
+ * z (m) and info may each be NULL. */
+int cxg_solver_solve(cxg_solver* solver, double* x, double* s, double* z, cxg_info* info);
+/* Solver::backward (new, no reference counterpart): given dL/dx (n) at the last Solved
+ * solution, returns dL/dq (n), dL/db (m), dL/d(values of P upper, in setup CSC order) and
+ * dL/d(values of A, in setup CSC order). Output pointers may be NULL. */
+int cxg_solver_backward(cxg_solver* solver, const double* dL_dx, double* dq, double* db,
+                        double* dPx, double* dAx);
+
+/* ---- batch of independent instances (new; no reference counterpart) --------------------- */
+typedef struct cxg_batch cxg_batch;
+
+/* Symbolic set-up of `count` instances (patterns fixed from here on). */
+int cxg_batch_create(cxg_batch** out, int count, const cxg_problem* problems,
+                     const cxg_settings* settings);
+void cxg_batch_destroy(cxg_batch* batch);
+int cxg_batch_count(const cxg_batch* batch);
+/* Sizes of the concatenated value/solution arrays: sum of nnz(P upper), n, nnz(A), m. */
+int cxg_batch_sizes(const cxg_batch* batch, int64_t* nnzP, int64_t* n_total, int64_t* nnzA,
+                    int64_t* m_total);
+/* Offsets of instance i inside the concatenated arrays (each may be NULL). */
+int cxg_batch_offsets(const cxg_batch* batch, int i, int64_t* pOff, int64_t* nOff, int64_t* aOff,
+                      int64_t* mOff);
+/* updateData for every instance at once from HOST arrays (concatenated in instance order;
+ * any may be NULL = unchanged). Values only: the patterns are those given at create time. */
+int cxg_batch_update_values(cxg_batch* batch, const double* Px, const double* q, const double* Ax,
+                            const double* b);
+/* Solve every instance; HOST outputs (concatenated x, s, z; info[count]); any may be NULL. */
+int cxg_batch_solve(cxg_batch* batch, double* x, double* s, double* z, cxg_info* info);
+/* Device-pointer variants: inputs/outputs are device buffers; work is enqueued on `stream`
+ * (a cudaStream_t, NULL = legacy default stream) and the call returns without synchronising. */
+int cxg_batch_update_values_device(cxg_batch* batch, const double* Px, const double* q,
+                                   const double* Ax, const double* b, void* stream);
+int cxg_batch_solve_device(cxg_batch* batch, double* x, double* s, double* z, cxg_info* info,
+                           void* stream);
+/* Adjoint of every instance at its last solution (see cxg_solver_backward); host arrays. */
+int cxg_batch_backward(cxg_batch* batch, const double* dL_dx, double* dq, double* db, double* dPx,
+                       double* dAx);
+int cxg_batch_backward_device(cxg_batch* batch, const double* dL_dx, double* dq, double* db,
+                              double* dPx, double* dAx, void* stream);
+/* Kernel launches enqueued by the last solve/backward call of this batch. */
+int cxg_batch_last_launches(const cxg_batch* batch);
+/* Device footprint of the batch in bytes: index plans + equilibration (plan), problem values +
+ * solutions + results (values), per-CTA working memory (scratch). Any pointer may be NULL. */
+int cxg_batch_footprint(const cxg_batch* batch, int64_t* plan_bytes, int64_t* value_bytes, int64_t* scratch_bytes);
+/* Human-readable launch configuration (one line per size bucket) into buf; returns the length. */
+int cxg_batch_describe(const cxg_batch* batch, char* buf, int buflen);
+
+/* ---- diagnostics (used by the parity tests) ---------------------------------------------- */
+/* Runs the IPM kernel's device cone algebra on one cone set K = Zero^zero x R^nn_+ x Q^... of
+ * total dimension m, after the Nesterov-Todd scaling of (s, z) (NonnegativeCone/SecondOrderCone
+ * ::updateScaling, src/conicxx/cones/nonnegative_cone.cpp:22-26, second_order_cone.cpp:70-159).
+ * op: 0 out = W u, 1 out = W^-1 u, 2 out = Hs u (ConeSet::applyW / applyWInv / mulHs,
+ * cone_set.cpp:56-75), 7 out = (Hs + eps I)^-1 u with eps = alpha_or_eps; 3 out = u o v,
+ * 4 out = u \ v (product / inverseProduct, cone_set.cpp:34-46); 5 scalars[0] = maxStep(u, v,
+ * alpha_or_eps) (cone_set.cpp:108-115); 6 scalars[0..1] = margins(u) (cone_set.cpp:77-90).
+ * soc_params (optional, 8 per SOC block): [kind, beta, lambda, q_c, q_s, ...] of the scaling. */
+int cxg_cones_eval(int op, int zero_dim, int nonneg_dim, int n_soc, const int* soc_dims, const double* s,
+                   const double* z, const double* u, const double* v, double alpha_or_eps, double* out,
+                   double* scalars, double* soc_params);
+/* Host equilibration of the set-up path (Equilibration::compute, src/conicxx/kkt/equilibration.cpp:8-100):
+ * d (n), e (m), c. No GPU needed. */
+int cxg_equilibration(const cxg_problem* problem, const cxg_settings* settings, double* d, double* e, double* c);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CONICXX_GB300_H */

@@ -1,0 +1,275 @@
+"""GPU parity tests: the CUDA path (through the C-ABI) against the CPU oracle and the reference's
+known answers.
+
+Criteria (FP64 oracle as the reference): same status; iteration count within +-1 (a GPU count
+lower than the oracle's by more is reported, as the reduced-KKT factorisation can converge
+where the reference's numerics stall); solutions within the stated relative tolerance; primal
+and dual residuals within tol_feas for Solved instances.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from conftest import kat_qp, rel
+from conicxx_gb300 import _abi, _lib, generators
+from conicxx_gb300._abi import dptr, iptr
+
+pytestmark = pytest.mark.gpu
+
+X_TOL = 1e-5  # relative x/s/z tolerance against the FP64 oracle (1e-8 gap stopping criteria)
+
+
+def _solvers():
+    from conicxx_gb300 import BatchSolver, Solver
+
+    return Solver, BatchSolver
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _need_gpu():
+    if _lib.lib().cxg_device_count() < 1:
+        pytest.fail("a CUDA device is required for the -m gpu tests")
+
+
+# ---- reference known-answer tests ------------------------------------------------------------
+@pytest.mark.parametrize("precision", [_abi.PRECISION_FP64, _abi.PRECISION_MIXED])
+@pytest.mark.parametrize("idx", range(8))
+def test_kats(kats, idx, precision):
+    Solver, _ = _solvers()
+    k = kats[idx]
+    qp = kat_qp(k)
+    S = Solver()
+    assert S.setup(qp, precision=precision)
+    sol = S.solve()
+    assert sol.status == k["status"], (k["name"], sol.status_name)
+    if k["x"] is not None:
+        assert np.allclose(sol.x, k["x"], atol=k["tol"]), (k["name"], sol.x)
+    if k["objective"] is not None:
+        assert abs(sol.objective - k["objective"]) < k["tol"]
+    if k["status"] == _abi.STATUS_SOLVED:
+        st, fe, sz = qp.kkt_residuals(sol.x, sol.s, sol.z)
+        tol = max(k["tol"], 1e-6)
+        assert st < tol and fe < tol and abs(sz) < tol
+
+
+def test_kats_as_one_batch(kats):
+    """All known-answer problems in one batched launch (mixed sizes and cone types)."""
+    _, BatchSolver = _solvers()
+    qps = [kat_qp(k) for k in kats]
+    B = BatchSolver(qps)
+    x, s, z, infos = B.solve()
+    for i, (xi, si, zi) in enumerate(B.split(x, s, z)):
+        k = kats[i]
+        assert infos[i]["status"] == k["status"], k["name"]
+        if k["x"] is not None:
+            assert np.allclose(xi, k["x"], atol=k["tol"]), k["name"]
+
+
+def _box(c):
+    from conicxx_gb300.problem import QP, Csc
+
+    n = len(c)
+    P = Csc.from_triplets(n, n, [(0, 0, 1.0), (1, 1, 1.0)])
+    A = Csc.from_triplets(n, n, [(0, 0, -1.0), (1, 1, -1.0)])
+    return QP(P, -np.asarray(c, float), A, np.zeros(n), nonneg=n)
+
+
+def test_update_reuse_and_pattern_mismatch():
+    """test/solver/test_update_reuse.cpp:32-89 through the C-ABI."""
+    from conicxx_gb300.problem import QP, Csc
+
+    Solver, _ = _solvers()
+    targets = [(1.0, 2.0), (-1.0, 3.0), (0.5, -0.5)]
+    S = Solver()
+    assert S.setup(_box(targets[0]))
+    for t, c in enumerate(targets):
+        p = _box(c)
+        if t > 0:
+            assert S.update_data(q=p.q)
+        sol = S.solve()
+        assert sol.ok()
+        F = Solver()
+        assert F.setup(p)
+        assert np.allclose(sol.x, F.solve().x, atol=1e-6)
+        assert np.allclose(sol.x, np.maximum(c, 0), atol=1e-6)
+    A_bad = Csc.from_triplets(2, 2, [(0, 0, -1.0), (0, 1, 0.3), (1, 1, -1.0)])
+    assert not S.update_data(A=A_bad)
+    assert S.setup(QP(_box((1.0, 1.0)).P, -np.ones(2), A_bad, np.zeros(2), nonneg=2))
+    assert S.solve().ok()
+
+
+def test_warm_start_and_update_data_matrices(oracle_mod):
+    """updateData of P and A values (same pattern) and an explicit setWarmStart against the oracle."""
+    Solver, _ = _solvers()
+    qp = generators.contact_qp(21, contacts=12)
+    qp2 = generators.contact_qp(22, contacts=12)
+    S = Solver()
+    assert S.setup(qp)
+    assert S.solve().ok()
+    if np.array_equal(qp.P.indptr, qp2.P.indptr) and np.array_equal(qp.P.indices, qp2.P.indices):
+        assert S.update_data(P=qp2.P, q=qp2.q)
+    else:
+        assert not S.update_data(P=qp2.P)  # pattern differs: rejected, like the reference
+    O = oracle_mod.OracleSolver()
+    assert O.setup(qp)
+    xo, so, zo, _ = O.solve()
+    S2 = Solver()
+    assert S2.setup(qp)
+    S2.set_warm_start(xo, so, zo)
+    O2 = oracle_mod.OracleSolver()
+    O2.setup(qp)
+    O2.set_warm_start(xo, so, zo)
+    sol = S2.solve()
+    x2, _, _, i2 = O2.solve()
+    assert sol.ok() and i2["status"] == 1
+    assert abs(sol.info["iterations"] - i2["iterations"]) <= 1
+    assert rel(sol.x, x2) < X_TOL
+
+
+# ---- device cone algebra against the oracle --------------------------------------------------
+def _interior(rng, zero, nn, soc, near=None):
+    parts = [np.zeros(zero), rng.uniform(0.2, 2.0, nn)]
+    for d in soc:
+        u1 = rng.standard_normal(d - 1)
+        gap = rng.uniform(0.05, 1.0) if near is None else near
+        parts.append(np.concatenate([[np.linalg.norm(u1) + gap], u1]))
+    return np.concatenate(parts)
+
+
+def _cones_eval(op, zero, nn, soc, s, z, u, v=None, a=0.0):
+    m = zero + nn + sum(soc)
+    socs = np.asarray(soc if soc else [1], np.int32)
+    out, sc, par = np.zeros(m), np.zeros(2), np.zeros(8 * max(len(soc), 1))
+    vv = np.ascontiguousarray(v if v is not None else u, dtype=np.float64)
+    s, z, u = (np.ascontiguousarray(t, dtype=np.float64) for t in (s, z, u))
+    rc = _lib.lib().cxg_cones_eval(op, zero, nn, len(soc), iptr(socs), dptr(s), dptr(z), dptr(u), dptr(vv), a,
+                                   dptr(out), dptr(sc), dptr(par))
+    assert rc == 0, _lib.lib().cxg_last_error()
+    return out, sc, par
+
+
+@pytest.mark.parametrize("soc", [[3] * 6, [2, 4, 17, 3], [1, 3, 5]])
+@pytest.mark.parametrize("near", [None, 1e-4, 1e-9])
+def test_cone_algebra_matches_oracle(oracle_mod, soc, near):
+    rng = np.random.default_rng(len(soc) * 7 + (0 if near is None else int(-np.log10(near))))
+    zero, nn = 2, 5
+    C_ = oracle_mod.OracleCones(zero, nn, soc)
+    s = _interior(rng, zero, nn, soc, near)
+    z = _interior(rng, zero, nn, soc, near)
+    u = rng.standard_normal(len(s))
+    v = rng.standard_normal(len(s))
+    C_.update_scaling(s, z)
+    _, Wcat, _ = C_.scaling()
+    conds, off = [1.0], 0
+    for d in soc:
+        conds.append(np.linalg.cond(Wcat[off:off + d * d].reshape(d, d)))
+        off += d * d
+    cond = max(conds)
+    for op, name in [(0, "apply_w"), (1, "apply_w_inv"), (2, "mul_hs")]:
+        g = _cones_eval(op, zero, nn, soc, s, z, u)[0]
+        o = C_.apply(name, u)
+        scale = max(np.abs(o).max(), 1e-300)
+        # the device eigen-form vs the oracle's dense W, W*W and LU(W): both are FP64-exact up to
+        # the conditioning of W, so they agree to ~cond(W)^2 * eps relative to the result's size
+        tol = 1e-12 + 1e-15 * cond * cond
+        assert np.abs(g - o).max() / scale < tol, (name, np.abs(g - o).max(), scale, cond)
+    for op, name in [(3, "product"), (4, "inverse_product")]:
+        g = _cones_eval(op, zero, nn, soc, s, z, s, v)[0]
+        o = C_.apply(name, s, v)
+        assert np.allclose(g, o, rtol=1e-10, atol=1e-10 * np.abs(o).max()), name
+    dx = rng.standard_normal(len(s))
+    g = _cones_eval(5, zero, nn, soc, s, z, s, dx, 10.0)[1][0]
+    assert abs(g - C_.max_step(s, dx, 10.0)) <= 1e-12 * max(1.0, abs(g))
+    g = _cones_eval(6, zero, nn, soc, s, z, u)[1]
+    mn, pos = C_.margins(u)
+    assert abs(g[0] - mn) < 1e-12 and abs(g[1] - pos) < 1e-12
+
+
+def test_cone_kats_on_device():
+    """test/cones/test_second_order_cone.cpp:46-119 and test_nonnegative_cone.cpp:33-71 on the
+    device cone functions."""
+    s, z = np.array([3.0, 1.0, 1.0]), np.array([2.0, 0.5, 0.5])
+    assert np.allclose(_cones_eval(2, 0, 0, [3], s, z, z)[0], s, atol=1e-10)  # Hs z = s
+    assert np.allclose(_cones_eval(1, 0, 0, [3], s, z, s)[0], _cones_eval(0, 0, 0, [3], s, z, z)[0], atol=1e-10)
+    e = np.array([1.0, 0, 0])
+    for dx, exp in [((-1.0, 0, 0), 1.0), ((1.0, 1.0, 0), 10.0), ((0.0, 1.0, 0), 1.0)]:
+        assert abs(_cones_eval(5, 0, 0, [3], e, e, e, np.array(dx), 10.0)[1][0] - exp) < 1e-12
+    sn, zn = np.array([1.0, 4, 0.5, 9]), np.array([2.0, 1, 2, 3])
+    assert np.allclose(_cones_eval(2, 0, 4, [], sn, zn, zn)[0], sn, atol=1e-12)
+    x, dxn = np.array([1.0, 2, 3]), np.array([-2.0, -1, 5])
+    assert abs(_cones_eval(5, 0, 3, [], x, x, x, dxn, 10.0)[1][0] - 0.5) < 1e-14
+
+
+def test_cone_identity_fallback_on_device(oracle_mod):
+    """Degenerate SOC blocks take the identity scaling exactly like second_order_cone.cpp:152-156."""
+    s = np.array([1.0, 1.0 - 1e-13, 0.0])  # numerically on the boundary
+    z = np.array([1e-3, 0.0, 0.0])
+    C_ = oracle_mod.OracleCones(0, 0, [3])
+    C_.update_scaling(s, z)
+    _, W, _ = C_.scaling()
+    u = np.array([0.3, -0.7, 1.1])
+    out, _, par = _cones_eval(0, 0, 0, [3], s, z, u)
+    if np.allclose(W.reshape(3, 3), np.eye(3)):
+        assert par[0] == 0.0 and np.allclose(out, u)
+    assert rel(out, C_.apply("apply_w", u)) < 1e-6
+
+
+# ---- instances: golden fixtures and live oracle ----------------------------------------------
+@pytest.mark.parametrize("precision", [_abi.PRECISION_FP64, _abi.PRECISION_MIXED])
+def test_golden_instances(golden_instances, precision):
+    Solver, _ = _solvers()
+    for name, qp, exp in golden_instances:
+        S = Solver()
+        assert S.setup(qp, precision=precision)
+        sol = S.solve()
+        assert sol.status == exp["status"], (name, sol.status_name)
+        assert abs(sol.info["iterations"] - exp["iterations"]) <= 1 or sol.info["iterations"] < exp["iterations"], \
+            (name, sol.info["iterations"], exp["iterations"])
+        for a, b in ((sol.x, exp["x"]), (sol.s, exp["s"]), (sol.z, exp["z"])):
+            assert rel(a, b) < X_TOL, (name, rel(a, b))
+        assert sol.info["primal_residual"] < 1e-8 and sol.info["dual_residual"] < 1e-8
+
+
+@pytest.mark.parametrize("family", ["contact", "cfg3"])
+def test_batch_against_live_oracle(oracle_mod, family):
+    _, BatchSolver = _solvers()
+    if family == "contact":
+        qps = [generators.contact_qp(1000 + i) for i in range(48)]
+    else:
+        qps = [generators.config3_qp(100 + i) for i in range(16)]
+    B = BatchSolver(qps)
+    x, s, z, infos = B.solve()
+    diffs = []
+    for i, (xi, si, zi) in enumerate(B.split(x, s, z)):
+        xo, so, zo, io, _ = oracle_mod.solve(qps[i])
+        assert infos[i]["status"] == io["status"], (i, infos[i]["status"], io["status"])
+        diffs.append(int(infos[i]["iterations"]) - io["iterations"])
+        if io["status"] == 1:
+            assert rel(xi, xo) < X_TOL, (i, rel(xi, xo))
+    diffs = np.array(diffs)
+    assert np.all(diffs <= 1), diffs
+    assert np.mean(np.abs(diffs) <= 1) >= 0.9, diffs
+
+
+def test_full_size_contact_batch_properties():
+    """4096 contact instances (c ~ U{4..64}): size-independent properties of every result --
+    definite statuses, and for Solved instances the original problem's KKT conditions, cone
+    membership of s and z, and the reported residuals within tolerance."""
+    _, BatchSolver = _solvers()
+    qps = generators.contact_batch(4096)
+    B = BatchSolver(qps, warm_start=0)
+    x, s, z, infos = B.solve()
+    st = infos["status"]
+    assert set(np.unique(st)) <= {1, 4}
+    assert np.mean(st == 1) > 0.99
+    for i, (xi, si, zi) in enumerate(B.split(x, s, z)):
+        if st[i] != 1:
+            continue
+        qp = qps[i]
+        a, b, c = qp.kkt_residuals(xi, si, zi)
+        scale = 1.0 + np.abs(qp.q).max()
+        assert a < 1e-5 * scale and b < 1e-5 * scale and abs(c) < 1e-5 * scale, (i, a, b, c)
+        assert qp.cone_margins(si)[0] > -1e-7 and qp.cone_margins(zi)[0] > -1e-7
+    ok = st == 1
+    assert np.all(infos["primal_residual"][ok] < 1e-8) and np.all(infos["dual_residual"][ok] < 1e-8)
