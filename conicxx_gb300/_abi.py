@@ -65,7 +65,7 @@ def default_settings(**overrides):
         refine_max_iter=3, refine_tol=1e-12, max_step_fraction=0.99, equilibrate=1,
         equilibrate_max_iter=10, equilibrate_min_scale=1e-4, equilibrate_max_scale=1e4,
         warm_start=1, verbose=0, record_timings=0, validate_inputs=1,
-        linear_solver=LINSOLVER_QDLDL, precision=PRECISION_FP64, mixed_refine_max_iter=6,
+        linear_solver=LINSOLVER_QDLDL, precision=PRECISION_FP64, mixed_refine_max_iter=4,
         mixed_fallback_tol=1e-10, threads_per_instance=0,
     )
     for k, v in overrides.items():

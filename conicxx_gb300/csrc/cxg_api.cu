@@ -90,7 +90,7 @@ extern "C" void cxg_default_settings(cxg_settings* s) {
   s->validate_inputs = 1;
   s->linear_solver = CXG_LINSOLVER_QDLDL;
   s->precision = CXG_PRECISION_FP64;
-  s->mixed_refine_max_iter = 6;
+  s->mixed_refine_max_iter = 4;
   s->mixed_fallback_tol = 1e-10;
   s->threads_per_instance = 0;
 }
@@ -130,6 +130,8 @@ struct cxg_batch {
   int* dCounters = nullptr;
   int* dOrder = nullptr;
   cudaStream_t stream = nullptr;
+  std::vector<cudaStream_t> groupStreams;   // one per size bucket (forked inside the graph)
+  std::vector<cudaEvent_t> forkJoin;        // fork event + one join event per bucket
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t graphExec = nullptr;
   DevSettings graphSettings{};
@@ -145,6 +147,8 @@ struct cxg_batch {
     void* ptrs[] = {dDesc, dIpool, dDpool, dPx, dq, dAx, db, dx, ds, dz, dRes, dWx, dWs, dWz, dHaveWarm, dScratch, dCounters, dOrder};
     for (void* p : ptrs)
       if (p) cudaFree(p);
+    for (cudaEvent_t e : forkJoin) cudaEventDestroy(e);
+    for (cudaStream_t gs : groupStreams) cudaStreamDestroy(gs);
     if (stream) cudaStreamDestroy(stream);
   }
 };
@@ -187,11 +191,12 @@ static int64_t r2(int64_t v) { return (v + 1) & ~int64_t(1); }
 
 // Group boundaries on the root dimension nr; each group gets a shared-memory layout sized for
 // its largest instance.
-static const int kBucketEdges[] = {48, 96, 144, 192, 256, 384, 512, 1024, 2048, 4096};
+static const int kBucketEdges[] = {32, 64, 96, 128, 160, 192, 256, 384, 512, 1024, 2048, 4096};
 
 static int chooseBlock(int nrMax, int requested) {
   if (requested == 64 || requested == 128 || requested == 256 || requested == 512) return requested;
-  if (nrMax <= 96) return 128;
+  if (nrMax <= 64) return 64;
+  if (nrMax <= 128) return 128;
   if (nrMax <= 512) return 256;
   return 512;
 }
@@ -464,11 +469,28 @@ extern "C" int cxg_batch_update_values_device(cxg_batch* B, const double* Px, co
   return copyValues(B, Px, q, Ax, b, cudaMemcpyDeviceToDevice, (cudaStream_t)stream);
 }
 
-// Enqueues the device-side solve sequence (queue resets + one persistent launch per group).
+// Enqueues the device-side solve sequence on `s`: queue resets, then one persistent launch per
+// size bucket, each on its own stream forked from and joined back into `s`, so the buckets run
+// concurrently and the batch waits for its slowest instance once rather than once per bucket.
 static int enqueueSolve(cxg_batch* B, cudaStream_t s) {
   const DevSettings ds = makeDevSettings(B->st, B->kktSt);
   CX_CUDA(cudaMemsetAsync(B->dCounters, 0, sizeof(int) * (B->groups.size() + 1), s));
-  for (const Group& g : B->groups) {
+  const size_t G = B->groups.size();
+  while (B->groupStreams.size() < G) {
+    cudaStream_t gs;
+    CX_CUDA(cudaStreamCreateWithFlags(&gs, cudaStreamNonBlocking));
+    B->groupStreams.push_back(gs);
+  }
+  while (B->forkJoin.size() < G + 1) {
+    cudaEvent_t e;
+    CX_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    B->forkJoin.push_back(e);
+  }
+  CX_CUDA(cudaEventRecord(B->forkJoin[0], s));
+  for (size_t gi = 0; gi < G; ++gi) {
+    const Group& g = B->groups[gi];
+    cudaStream_t gs = (G == 1) ? s : B->groupStreams[gi];
+    if (G > 1) CX_CUDA(cudaStreamWaitEvent(gs, B->forkJoin[0], 0));
     LaunchArgs a{};
     a.desc = B->dDesc;
     a.order = B->dOrder + g.begin;
@@ -492,9 +514,13 @@ static int enqueueSolve(cxg_batch* B, cudaStream_t s) {
     a.scratchStride = g.stride;
     a.st = ds;
     a.lay = g.lay;
-    CX_CUDA(launchIpm(a, g.grid, g.block, g.smem, g.fp32, s));
+    CX_CUDA(launchIpm(a, g.grid, g.block, g.smem, g.fp32, gs));
+    if (G > 1) {
+      CX_CUDA(cudaEventRecord(B->forkJoin[gi + 1], gs));
+      CX_CUDA(cudaStreamWaitEvent(s, B->forkJoin[gi + 1], 0));
+    }
   }
-  B->lastLaunches = (int)B->groups.size();
+  B->lastLaunches = (int)G;
   return CXG_OK;
 }
 

@@ -27,7 +27,8 @@ constexpr double kWMax = 1e8;                      // second_order_cone.cpp:152
 
 // Per-SOC-block scaling parameters (8 doubles in shared memory):
 // [0] kind (0 identity fallback, 1 diagonal, 2 plane), [1] beta, [2] lambda (plane) or
-// a = 2v0^2-1 (diagonal), [3] q1c, [4] q1s (in-plane eigenvector of lambda), [5..7] unused.
+// a = 2v0^2-1 (diagonal), [3] q1c, [4] q1s (in-plane eigenvector of lambda), [5..7] the three
+// eigenvalues of G = (Hs + eps I)^-1 prepared at factorisation time (socPrepareG).
 // The unit vector u is kept in a row-indexed array at rows off+1 .. off+dim-1.
 struct SocScale {
   double kind, beta, lam, qc, qs, r0, r1, r2;
@@ -147,6 +148,48 @@ __device__ __forceinline__ void socApply(const SocScale& sc, const double* u, in
   const double y0 = f1 * c1 * sc.qc - f2 * c2 * sc.qs;
   const double yF = f1 * c1 * sc.qs + f2 * c2 * sc.qc;
   for (int i = 1; i < d; ++i) y[i] = f3 * (x[i] - xf * u[i]) + yF * u[i];
+  y[0] = y0;
+}
+
+// G = (Hs + eps I)^-1 of one SOC block as its three eigenvalues (stored in sc.r0..r2).
+__device__ __forceinline__ void socPrepareG(SocScale& sc, double eps) {
+  const int kind = (int)sc.kind;
+  if (kind == 0) {
+    const double g = 1.0 / (1.0 + eps);
+    sc.r0 = sc.r1 = sc.r2 = g;
+  } else if (kind == 1) {
+    const double w0 = sc.beta * sc.lam, w = sc.beta;
+    sc.r0 = 1.0 / (w0 * w0 + eps);
+    sc.r1 = sc.r2 = 1.0 / (w * w + eps);
+  } else {
+    const double w1 = sc.beta * sc.lam, w2 = sc.beta / sc.lam, w3 = sc.beta;
+    sc.r0 = 1.0 / (w1 * w1 + eps);
+    sc.r1 = 1.0 / (w2 * w2 + eps);
+    sc.r2 = 1.0 / (w3 * w3 + eps);
+  }
+}
+
+// y = G x with the eigenvalues prepared by socPrepareG (same structure as socApply).
+__device__ __forceinline__ void socApplyG(const SocScale& sc, const double* u, int d, const double* x, double* y) {
+  const int kind = (int)sc.kind;
+  if (kind == 0) {
+    for (int i = 0; i < d; ++i) y[i] = sc.r0 * x[i];
+    return;
+  }
+  if (kind == 1) {
+    const double x0 = x[0];
+    for (int i = 1; i < d; ++i) y[i] = sc.r1 * x[i];
+    y[0] = sc.r0 * x0;
+    return;
+  }
+  const double x0 = x[0];
+  double xf = 0.0;
+  for (int i = 1; i < d; ++i) xf += u[i] * x[i];
+  const double c1 = sc.qc * x0 + sc.qs * xf;
+  const double c2 = -sc.qs * x0 + sc.qc * xf;
+  const double y0 = sc.r0 * c1 * sc.qc - sc.r1 * c2 * sc.qs;
+  const double yF = sc.r0 * c1 * sc.qs + sc.r1 * c2 * sc.qc;
+  for (int i = 1; i < d; ++i) y[i] = sc.r2 * (x[i] - xf * u[i]) + yF * u[i];
   y[0] = y0;
 }
 

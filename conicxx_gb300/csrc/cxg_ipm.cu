@@ -21,6 +21,11 @@ namespace cxg {
 
 #define FOR_T(i, n) for (int i = (int)threadIdx.x; i < (n); i += (int)blockDim.x)
 
+// Finiteness by the exponent bits (an integer test; FP64 compares run on the scarce FP64 pipe).
+__device__ __forceinline__ bool finiteBits(double v) {
+  return ((__double_as_longlong(v) >> 52) & 0x7ff) != 0x7ff;
+}
+
 // ------------------------------------------------------------------------------------------
 // block reductions (deterministic: fixed summation order, identical result in every thread)
 // ------------------------------------------------------------------------------------------
@@ -159,6 +164,22 @@ __device__ __noinline__ void coneApply(Ctx& c, int f, double eps, const double* 
       const int b = t - c.l;
       const int off = c.socOff[b], d = c.socDim[b];
       socApply(c.sp[b], c.cu + off, d, f, eps, x + off, out + off);
+    }
+  }
+  __syncthreads();
+}
+
+// out = G x on the cone rows with the G eigenvalues prepared at factorisation (Zero rows: 0).
+__device__ __noinline__ void coneApplyG(Ctx& c, const double* x, double* out) {
+  FOR_T(r, c.p) out[r] = 0.0;
+  FOR_T(t, c.l + c.nsoc) {
+    if (t < c.l) {
+      const int r = c.p + t;
+      out[r] = c.cu[r] * x[r];
+    } else {
+      const int b = t - c.l;
+      const int off = c.socOff[b], d = c.socDim[b];
+      socApplyG(c.sp[b], c.cu + off, d, x + off, out + off);
     }
   }
   __syncthreads();
@@ -552,17 +573,20 @@ __device__ __noinline__ void assembleFactor(Ctx& c, const DevSettings& st, T* M,
   const InstanceDesc& D = *c.D;
   const int n = c.n, nr = c.nr;
   const double epsA = st.static_reg_A + ea;
-  // T_u = G_u Ad_u with G_u = (Hs_u + epsA I)^-1, column by column
+  // G_u = (Hs_u + epsA I)^-1 as eigenvalues (NN: cu[row]; SOC: sp.r0..r2), then
+  // T_u = G_u Ad_u column by column
   FOR_T(u, c.nUnits) {
     const int a0 = c.unitAd[u], a1 = c.unitAd[u + 1];
     if (u < c.l) {
       const double w = c.cw[c.p + u];
       const double g = 1.0 / (w * w + epsA);
+      c.cu[c.p + u] = g;
       for (int k = a0; k < a1; ++k) c.T[k] = g * c.Ad[k];
     } else {
       const int b = u - c.l;
       const int off = c.socOff[b], d = c.socDim[b];
-      for (int k = a0; k < a1; k += d) socApply(c.sp[b], c.cu + off, d, kGinv, epsA, c.Ad + k, c.T + k);
+      socPrepareG(c.sp[b], epsA);
+      for (int k = a0; k < a1; k += d) socApplyG(c.sp[b], c.cu + off, d, c.Ad + k, c.T + k);
     }
   }
   const int64_t rs = rootSize(nr);
@@ -597,8 +621,8 @@ __device__ __noinline__ void reducedSolve(Ctx& c, const DevSettings& st, const T
   const double epsA = st.static_reg_A + ea;
   const double* r1 = rhs;
   const double* r2 = rhs + n;
-  // u = G_C r2_C
-  coneApply(c, kGinv, epsA, r2, c.tm);
+  // u = G_C r2_C (eigenvalues of G prepared at factorisation time)
+  coneApplyG(c, r2, c.tm);
   // t = [r1 + A_C' u ; r2_Z] in T precision
   T* y = reinterpret_cast<T*>(c.rr);
   FOR_T(j, n) {
@@ -628,16 +652,16 @@ __device__ __noinline__ void reducedSolve(Ctx& c, const DevSettings& st, const T
   FOR_T(t, c.l + c.nsoc) {
     if (t < c.l) {
       const int r = p + t;
-      const double w = c.cw[r];
-      sol[n + r] = c.tm[r] / (w * w + epsA);
+      sol[n + r] = c.tm[r] * c.cu[r];
     } else {
       const int b = t - c.l;
       const int off = c.socOff[b], d = c.socDim[b];
-      socApply(c.sp[b], c.cu + off, d, kGinv, epsA, c.tm + off, sol + n + off);
+      socApplyG(c.sp[b], c.cu + off, d, c.tm + off, sol + n + off);
     }
   }
   __syncthreads();
   (void)nr;
+  (void)epsA;
 }
 
 // Factorisation state of the current iteration.
@@ -690,7 +714,7 @@ __device__ void solveOnce(Ctx& c, const DevSettings& st, const FactState& fs, co
 
 __device__ __noinline__ bool vecFinite(Ctx& c, const double* v, int len) {
   int bad = 0;
-  FOR_T(i, len) if (!isfinite(v[i])) bad = 1;
+  FOR_T(i, len) bad |= !finiteBits(v[i]);
   return blockOrInt(bad, c.redi) == 0;
 }
 
@@ -726,14 +750,19 @@ __device__ __noinline__ double kktSolveImpl(Ctx& c, const DevSettings& st, FactS
     }
     double rhsNorm = 1.0;
     double rel = kktResidual(c, st, rhs, sol, c.res, rhsNorm);
-    const int maxRef = (sizeof(FT) == 4 && !fs.use64) ? st.mixed_refine_max_iter : st.refine_max_iter;
+    const bool fp32Factor = (sizeof(FT) == 4) && !fs.use64;
+    const int maxRef = fp32Factor ? st.mixed_refine_max_iter : st.refine_max_iter;
     int steps = 0;
     for (int it = 0; it < maxRef && rel > st.refine_tol; ++it) {
       solveOnce<FT>(c, st, fs, c.res, c.cor);
       FOR_T(i, N) sol[i] += c.cor[i];
       __syncthreads();
+      const double prev = rel;
       rel = kktResidual(c, st, rhs, sol, c.res, rhsNorm);
       ++steps;
+      // an FP32 factor whose refinement contracts by less than 4x per step will not reach the
+      // tolerance in the remaining steps: go to the FP64 factor now
+      if (fp32Factor && !(rel <= st.mixed_fallback_tol) && !(rel <= 0.25 * prev)) break;
     }
     if (threadIdx.x == 0) c.sc[SC_RSTEPS] += steps;
     const bool mixedFp32 = (sizeof(FT) == 4) && !fs.use64;
@@ -835,8 +864,8 @@ __device__ __noinline__ void solveInstance(Ctx& c, const LaunchArgs& a, int inst
       shiftToInteriorCold(c, c.s, degree);
       shiftToInteriorCold(c, c.z, degree);
       int bad = 0;
-      FOR_T(j, n) if (!isfinite(c.x[j])) bad = 1;
-      FOR_T(r, m) if (!isfinite(c.s[r]) || !isfinite(c.z[r])) bad = 1;
+      FOR_T(j, n) bad |= !finiteBits(c.x[j]);
+      FOR_T(r, m) bad |= !finiteBits(c.s[r]) | !finiteBits(c.z[r]);
       initOk = blockOrInt(bad, c.redi) == 0;
     }
   }
@@ -945,9 +974,9 @@ __device__ __noinline__ void solveInstance(Ctx& c, const LaunchArgs& a, int inst
       __syncthreads();
       const double dkappaA = -(dkrA + kappa * dtauA) / tau;
       {
-        int bad = !isfinite(dtauA) || !isfinite(dkappaA);
-        FOR_T(j, n) if (!isfinite(c.dx[j])) bad = 1;
-        FOR_T(r, m) if (!isfinite(c.dz[r]) || !isfinite(c.ds[r])) bad = 1;
+        int bad = !finiteBits(dtauA) || !finiteBits(dkappaA);
+        FOR_T(j, n) bad |= !finiteBits(c.dx[j]);
+        FOR_T(r, m) bad |= !finiteBits(c.dz[r]) | !finiteBits(c.ds[r]);
         if (blockOrInt(bad, c.redi)) { status = 5; break; }
       }
       // 6. affine step length (no fraction), mu_aff, sigma
@@ -1004,9 +1033,9 @@ __device__ __noinline__ void solveInstance(Ctx& c, const LaunchArgs& a, int inst
       __syncthreads();
       const double dkappa = -(dkrC + kappa * dtau) / tau;
       {
-        int bad = !isfinite(dtau) || !isfinite(dkappa);
-        FOR_T(j, n) if (!isfinite(c.dx[j])) bad = 1;
-        FOR_T(r, m) if (!isfinite(c.dz[r]) || !isfinite(c.ds[r])) bad = 1;
+        int bad = !finiteBits(dtau) || !finiteBits(dkappa);
+        FOR_T(j, n) bad |= !finiteBits(c.dx[j]);
+        FOR_T(r, m) bad |= !finiteBits(c.dz[r]) | !finiteBits(c.ds[r]);
         if (blockOrInt(bad, c.redi)) { status = 5; break; }
       }
       // 8. step length with the fraction-to-boundary factor

@@ -86,7 +86,8 @@ typedef struct cxg_settings {
   /* ---- GB300 additions ---- */
   int precision;              /* CXG_PRECISION_FP64 for cxg_solver, MIXED for cxg_batch */
   int mixed_refine_max_iter;  /* refinement steps allowed on an FP32 factor before the FP64
-                                 refactorisation fallback (default 6) */
+                                 refactorisation fallback (default 4; a step contracting the
+                                 residual by less than 4x falls back at once) */
   double mixed_fallback_tol;  /* relative KKT residual above which an FP32-factor solve is redone
                                  with an FP64 factor (default 1e-10) */
   int threads_per_instance;   /* 0 = autotuned; else 64/128/256/512 */

@@ -17,7 +17,11 @@ from conicxx_gb300._abi import dptr, iptr
 
 pytestmark = pytest.mark.gpu
 
-X_TOL = 1e-5  # relative x/s/z tolerance against the FP64 oracle (1e-8 gap stopping criteria)
+# Relative tolerance of GPU vs FP64-oracle solutions. Both runs stop at the 1e-8 residual/gap
+# tests, so their final iterates differ by what that stopping rule leaves undetermined: measured
+# up to ~2e-6 for x and ~2e-5 for the duals z (and s) on the contact instances.
+X_TOL = 1e-5
+SZ_TOL = 1e-4
 
 
 def _solvers():
@@ -174,10 +178,16 @@ def test_cone_algebra_matches_oracle(oracle_mod, soc, near):
         # the conditioning of W, so they agree to ~cond(W)^2 * eps relative to the result's size
         tol = 1e-12 + 1e-15 * cond * cond
         assert np.abs(g - o).max() / scale < tol, (name, np.abs(g - o).max(), scale, cond)
-    for op, name in [(3, "product"), (4, "inverse_product")]:
+    # the inverse Jordan product divides by rho = u0^2 - |u1|^2: its conditioning is u0^2/|rho|
+    cond_ip, off = 1.0, zero + nn
+    for d in soc:
+        ub = s[off:off + d]
+        cond_ip = max(cond_ip, ub[0] ** 2 / max(abs(ub[0] ** 2 - ub[1:] @ ub[1:]), 1e-300))
+        off += d
+    for op, name, tol in [(3, "product", 1e-12), (4, "inverse_product", 1e-12 * cond_ip)]:
         g = _cones_eval(op, zero, nn, soc, s, z, s, v)[0]
         o = C_.apply(name, s, v)
-        assert np.allclose(g, o, rtol=1e-10, atol=1e-10 * np.abs(o).max()), name
+        assert np.abs(g - o).max() <= tol * max(np.abs(o).max(), 1.0), (name, np.abs(g - o).max(), cond_ip)
     dx = rng.standard_normal(len(s))
     g = _cones_eval(5, zero, nn, soc, s, z, s, dx, 10.0)[1][0]
     assert abs(g - C_.max_step(s, dx, 10.0)) <= 1e-12 * max(1.0, abs(g))
@@ -226,8 +236,8 @@ def test_golden_instances(golden_instances, precision):
         assert sol.status == exp["status"], (name, sol.status_name)
         assert abs(sol.info["iterations"] - exp["iterations"]) <= 1 or sol.info["iterations"] < exp["iterations"], \
             (name, sol.info["iterations"], exp["iterations"])
-        for a, b in ((sol.x, exp["x"]), (sol.s, exp["s"]), (sol.z, exp["z"])):
-            assert rel(a, b) < X_TOL, (name, rel(a, b))
+        for a, b, tol in ((sol.x, exp["x"], X_TOL), (sol.s, exp["s"], SZ_TOL), (sol.z, exp["z"], SZ_TOL)):
+            assert rel(a, b) < tol, (name, rel(a, b))
         assert sol.info["primal_residual"] < 1e-8 and sol.info["dual_residual"] < 1e-8
 
 
@@ -269,7 +279,10 @@ def test_full_size_contact_batch_properties():
         qp = qps[i]
         a, b, c = qp.kkt_residuals(xi, si, zi)
         scale = 1.0 + np.abs(qp.q).max()
-        assert a < 1e-5 * scale and b < 1e-5 * scale and abs(c) < 1e-5 * scale, (i, a, b, c)
+        obj = abs(infos[i]["objective"])
+        # stationarity/feasibility absolute; complementarity relative to the objective (the
+        # stopping rule is a relative gap, src/conicxx/solver_impl.cpp checkConvergence)
+        assert a < 1e-5 * scale and b < 1e-5 * scale and abs(c) < 1e-6 * max(1.0, obj), (i, a, b, c, obj)
         assert qp.cone_margins(si)[0] > -1e-7 and qp.cone_margins(zi)[0] > -1e-7
     ok = st == 1
     assert np.all(infos["primal_residual"][ok] < 1e-8) and np.all(infos["dual_residual"][ok] < 1e-8)
