@@ -209,6 +209,48 @@ def run_gb300(args, rank, world, local_rank):
             S.solve()
         plain_s = time.perf_counter() - p0
         plain_rate = plain_n / plain_s
+        # ---- differentiable layer: 1024 instances n=100, m=150 (Zero^10 x R^100_+ x 10 Q^4),
+        # forward alone vs forward + adjoint (dL/dq, dL/db, dL/dP, dL/dA for L = 1/2|x - t|^2) ----
+        dqps = generators.config3_batch(1024)
+        DB = BatchSolver(dqps, settings=default_settings(precision=1, warm_start=0, differentiable=1))
+        dv = [torch.from_numpy(v).to(dev) for v in DB.concat_values()]
+        dxx = torch.empty(DB.n_total, dtype=torch.float64, device=dev)
+        dss = torch.empty(DB.m_total, dtype=torch.float64, device=dev)
+        dzz = torch.empty(DB.m_total, dtype=torch.float64, device=dev)
+        tgt = torch.from_numpy(np.concatenate([generators.x_target(i, q_.n) for i, q_ in enumerate(dqps)])).to(dev)
+        gq = torch.empty(DB.n_total, dtype=torch.float64, device=dev)
+        gbb = torch.empty(DB.m_total, dtype=torch.float64, device=dev)
+        gP = torch.empty(DB.nnzP, dtype=torch.float64, device=dev)
+        gA = torch.empty(DB.nnzA, dtype=torch.float64, device=dev)
+
+        def fwd():
+            DB.update_values_device(*(int(t.data_ptr()) for t in dv), sp)
+            DB.solve_device(int(dxx.data_ptr()), int(dss.data_ptr()), int(dzz.data_ptr()), sp)
+
+        def bwd():
+            gx = dxx - tgt
+            DB.backward_device(int(gx.data_ptr()), int(gq.data_ptr()), int(gbb.data_ptr()), int(gP.data_ptr()),
+                               int(gA.data_ptr()), sp)
+
+        with torch.cuda.stream(stream):
+            for _ in range(2):
+                fwd()
+                bwd()
+            torch.cuda.synchronize()
+            e = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+            fw, fb = [], []
+            for _ in range(max(2, args.steps)):
+                e[0].record(stream)
+                fwd()
+                e[1].record(stream)
+                bwd()
+                e[2].record(stream)
+                torch.cuda.synchronize()
+                fw.append(e[0].elapsed_time(e[1]))
+                fb.append(e[0].elapsed_time(e[2]))
+        fwd_bwd = {"instances": 1024, "workload": "n=100, m=150, Zero^10 x R^100_+ x 10 Q^4, L=1/2|x-t|^2",
+                   "fwd_us": 1e3 * float(np.median(fw)), "fwd_bwd_us": 1e3 * float(np.median(fb)),
+                   "ratio": float(np.median(fb) / np.median(fw))}
         # ---- CPU baseline: oracle restatement on the host cores ----
         sys.path.insert(0, os.path.join(ROOT, "oracle"))
         import oracle as orc
@@ -239,6 +281,7 @@ def run_gb300(args, rank, world, local_rank):
                       "frac": achieved / hbm_peak, "traffic": traffic, "peak_kind": peak_kind,
                       "note": "IPM kernel; HBM bytes = problem data + plans + solutions per launch; the kernel "
                               "is bound by the FP64 pipe and barrier latency, not HBM (see profiles/)"},
+            fwd_bwd=fwd_bwd,
             setup_s=setup_s,
         )
     return ms, wall, clocks, launches_per_step, solved_frac, statuses, result

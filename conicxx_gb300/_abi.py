@@ -54,6 +54,7 @@ class Settings(C.Structure):
         ("mixed_refine_max_iter", C.c_int),
         ("mixed_fallback_tol", C.c_double),
         ("threads_per_instance", C.c_int),
+        ("differentiable", C.c_int),
     ]
 
 
@@ -66,7 +67,7 @@ def default_settings(**overrides):
         equilibrate_max_iter=10, equilibrate_min_scale=1e-4, equilibrate_max_scale=1e4,
         warm_start=1, verbose=0, record_timings=0, validate_inputs=1,
         linear_solver=LINSOLVER_QDLDL, precision=PRECISION_FP64, mixed_refine_max_iter=4,
-        mixed_fallback_tol=1e-10, threads_per_instance=0,
+        mixed_fallback_tol=1e-10, threads_per_instance=0, differentiable=0,
     )
     for k, v in overrides.items():
         if not hasattr(s, k):

@@ -127,6 +127,9 @@ struct cxg_batch {
   double *dWx = nullptr, *dWs = nullptr, *dWz = nullptr;
   unsigned char* dHaveWarm = nullptr;
   double* dScratch = nullptr;
+  double* dBwd = nullptr;                 // saved final states (differentiable)
+  double *dGx = nullptr, *dGq = nullptr, *dGb = nullptr, *dGP = nullptr, *dGA = nullptr;
+  int64_t bwdTotal = 0;
   int* dCounters = nullptr;
   int* dOrder = nullptr;
   cudaStream_t stream = nullptr;
@@ -144,7 +147,8 @@ struct cxg_batch {
   ~cxg_batch() {
     if (graphExec) cudaGraphExecDestroy(graphExec);
     if (graph) cudaGraphDestroy(graph);
-    void* ptrs[] = {dDesc, dIpool, dDpool, dPx, dq, dAx, db, dx, ds, dz, dRes, dWx, dWs, dWz, dHaveWarm, dScratch, dCounters, dOrder};
+    void* ptrs[] = {dDesc, dIpool, dDpool, dPx, dq, dAx, db, dx, ds, dz, dRes, dWx, dWs, dWz, dHaveWarm, dScratch,
+                    dCounters, dOrder, dBwd, dGx, dGq, dGb, dGP, dGA};
     for (void* p : ptrs)
       if (p) cudaFree(p);
     for (cudaEvent_t e : forkJoin) cudaEventDestroy(e);
@@ -330,6 +334,14 @@ static int uploadPlan(cxg_batch* B) {
   if ((rc = devAlloc(&B->dHaveWarm, N))) return rc;
   if ((rc = devAlloc(&B->dCounters, B->groups.size() + 1))) return rc;
   if ((rc = devAlloc(&B->dOrder, N))) return rc;
+  if (B->st.differentiable) {
+    if ((rc = devAlloc(&B->dBwd, (size_t)B->bwdTotal))) return rc;
+    if ((rc = devAlloc(&B->dGx, (size_t)B->pools.totQ))) return rc;
+    if ((rc = devAlloc(&B->dGq, (size_t)B->pools.totQ))) return rc;
+    if ((rc = devAlloc(&B->dGb, (size_t)B->pools.totB))) return rc;
+    if ((rc = devAlloc(&B->dGP, (size_t)B->pools.totPx))) return rc;
+    if ((rc = devAlloc(&B->dGA, (size_t)B->pools.totAx))) return rc;
+  }
   CX_CUDA(cudaMemcpy(B->dDesc, B->pools.desc.data(), N * sizeof(InstanceDesc), cudaMemcpyHostToDevice));
   if (!B->pools.ipool.empty())
     CX_CUDA(cudaMemcpy(B->dIpool, B->pools.ipool.data(), B->pools.ipool.size() * sizeof(int), cudaMemcpyHostToDevice));
@@ -388,6 +400,14 @@ extern "C" int cxg_batch_create(cxg_batch** out, int count, const cxg_problem* p
   } catch (const std::exception& ex) {
     delete B;
     return setErr(CXG_E_NOMEM, std::string("planning failed: ") + ex.what());
+  }
+  if (st.differentiable) {
+    int64_t off = 0;
+    for (InstanceDesc& D : B->pools.desc) {
+      D.bwdOff = off;
+      off += bwdLayout(D.nr, D.n, D.m, D.nsoc).total;
+    }
+    B->bwdTotal = off;
   }
   int rc = CXG_OK;
   if (cudaStreamCreateWithFlags(&B->stream, cudaStreamNonBlocking) != cudaSuccess) {
@@ -510,6 +530,7 @@ static int enqueueSolve(cxg_batch* B, cudaStream_t s) {
     a.warmS = B->dWs;
     a.warmZ = B->dWz;
     a.haveWarm = B->dHaveWarm;
+    a.bwd = B->dBwd;
     a.scratch = B->dScratch + g.scratchOff;
     a.scratchStride = g.stride;
     a.st = ds;
@@ -673,7 +694,10 @@ extern "C" int cxg_solver_setup(cxg_solver* S, const cxg_problem* pr, const cxg_
   S->batch = nullptr;
   cxg_settings st;
   if (settings) st = *settings;
-  else cxg_default_settings(&st);
+  else {
+    cxg_default_settings(&st);
+    st.differentiable = 1;
+  }
   S->st = st;
   int rc = cxg_batch_create(&S->batch, 1, pr, &st);
   if (rc) return rc;
@@ -761,13 +785,77 @@ extern "C" int cxg_solver_backward(cxg_solver* S, const double* dL_dx, double* d
   return cxg_batch_backward(S->batch, dL_dx, dq, db, dPx, dAx);
 }
 
+extern "C" int cxg_batch_backward(cxg_batch* B, const double* dL_dx, double* dq, double* db, double* dPx, double* dAx);
+
+// Enqueues the adjoint of every instance (one launch per size bucket, forked like the solve).
+static int enqueueAdjoint(cxg_batch* B, cudaStream_t s, const double* gx, double* gq, double* gb, double* gP,
+                          double* gA) {
+  const DevSettings ds = makeDevSettings(B->st, B->kktSt);
+  CX_CUDA(cudaMemsetAsync(B->dCounters, 0, sizeof(int) * (B->groups.size() + 1), s));
+  const size_t G = B->groups.size();
+  CX_CUDA(cudaEventRecord(B->forkJoin[0], s));
+  for (size_t gi = 0; gi < G; ++gi) {
+    const Group& g = B->groups[gi];
+    cudaStream_t gs = (G == 1) ? s : B->groupStreams[gi];
+    if (G > 1) CX_CUDA(cudaStreamWaitEvent(gs, B->forkJoin[0], 0));
+    LaunchArgs a{};
+    a.desc = B->dDesc;
+    a.order = B->dOrder + g.begin;
+    a.count = g.count;
+    a.counter = B->dCounters + g.counterIdx;
+    a.ipool = B->dIpool;
+    a.dpool = B->dDpool;
+    a.Px = B->dPx;
+    a.q = B->dq;
+    a.Ax = B->dAx;
+    a.b = B->db;
+    a.bwd = B->dBwd;
+    a.gx = gx;
+    a.gq = gq;
+    a.gb = gb;
+    a.gP = gP;
+    a.gA = gA;
+    a.scratch = B->dScratch + g.scratchOff;
+    a.scratchStride = g.stride;
+    a.st = ds;
+    a.lay = g.lay;
+    CX_CUDA(launchAdjoint(a, g.grid, g.block, g.smem, gs));
+    if (G > 1) {
+      CX_CUDA(cudaEventRecord(B->forkJoin[gi + 1], gs));
+      CX_CUDA(cudaStreamWaitEvent(s, B->forkJoin[gi + 1], 0));
+    }
+  }
+  B->lastLaunches = (int)G;
+  return CXG_OK;
+}
+
+static int checkDifferentiable(cxg_batch* B) {
+  if (!B) return setErr(CXG_E_INVALID, "null batch");
+  if (!B->dBwd) return setErr(CXG_E_NOT_SETUP, "backward needs settings.differentiable = 1 at set-up");
+  if (B->forkJoin.empty()) return setErr(CXG_E_NOT_SETUP, "backward before any solve");
+  return CXG_OK;
+}
+
 extern "C" int cxg_batch_backward(cxg_batch* B, const double* dL_dx, double* dq, double* db, double* dPx, double* dAx) {
-  (void)B; (void)dL_dx; (void)dq; (void)db; (void)dPx; (void)dAx;
-  return setErr(CXG_E_UNSUPPORTED, "backward is not built yet");
+  int rc = checkDifferentiable(B);
+  if (rc) return rc;
+  if (!dL_dx) return setErr(CXG_E_INVALID, "null dL/dx");
+  CX_CUDA(cudaMemcpyAsync(B->dGx, dL_dx, (size_t)B->pools.totQ * 8, cudaMemcpyHostToDevice, B->stream));
+  rc = enqueueAdjoint(B, B->stream, B->dGx, B->dGq, B->dGb, B->dGP, B->dGA);
+  if (rc) return rc;
+  if (dq && B->pools.totQ) CX_CUDA(cudaMemcpyAsync(dq, B->dGq, (size_t)B->pools.totQ * 8, cudaMemcpyDeviceToHost, B->stream));
+  if (db && B->pools.totB) CX_CUDA(cudaMemcpyAsync(db, B->dGb, (size_t)B->pools.totB * 8, cudaMemcpyDeviceToHost, B->stream));
+  if (dPx && B->pools.totPx) CX_CUDA(cudaMemcpyAsync(dPx, B->dGP, (size_t)B->pools.totPx * 8, cudaMemcpyDeviceToHost, B->stream));
+  if (dAx && B->pools.totAx) CX_CUDA(cudaMemcpyAsync(dAx, B->dGA, (size_t)B->pools.totAx * 8, cudaMemcpyDeviceToHost, B->stream));
+  CX_CUDA(cudaStreamSynchronize(B->stream));
+  return CXG_OK;
 }
 
 extern "C" int cxg_batch_backward_device(cxg_batch* B, const double* dL_dx, double* dq, double* db, double* dPx,
                                          double* dAx, void* stream) {
-  (void)B; (void)dL_dx; (void)dq; (void)db; (void)dPx; (void)dAx; (void)stream;
-  return setErr(CXG_E_UNSUPPORTED, "backward is not built yet");
+  int rc = checkDifferentiable(B);
+  if (rc) return rc;
+  if (!dL_dx) return setErr(CXG_E_INVALID, "null dL/dx");
+  return enqueueAdjoint(B, (cudaStream_t)stream, dL_dx, dq ? dq : B->dGq, db ? db : B->dGb, dPx ? dPx : B->dGP,
+                        dAx ? dAx : B->dGA);
 }

@@ -1082,6 +1082,32 @@ __device__ __noinline__ void solveInstance(Ctx& c, const LaunchArgs& a, int inst
     a.s[D.vS + r] = eq ? (c.s[r] * scale) / evec[r] : c.s[r] * scale;
     a.z[D.vZ + r] = eq ? (c.z[r] * scale) * evec[r] / cs : c.z[r] * scale;
   }
+  if (a.bwd) {
+    // final factorisation (as FP64), scaling and normalised iterate for the adjoint
+    double* Bs = a.bwd + D.bwdOff;
+    const BwdLayout bl = bwdLayout(c.nr, n, m, c.nsoc);
+    const int64_t rs = rootSize(c.nr);
+    if (fs.use64 || sizeof(FT) == 8) {
+      const double* R = fs.use64 ? c.root64 : reinterpret_cast<const double*>(c.root);
+      for (int64_t t = threadIdx.x; t < rs; t += blockDim.x) Bs[bl.root + t] = R[t];
+    } else {
+      const FT* R = rootT<FT>(c);
+      for (int64_t t = threadIdx.x; t < rs; t += blockDim.x) Bs[bl.root + t] = (double)R[t];
+    }
+    FOR_T(r, m) {
+      Bs[bl.cw + r] = c.cw[r];
+      Bs[bl.cu + r] = c.cu[r];
+      Bs[bl.zh + r] = c.z[r] / tau;
+    }
+    FOR_T(k, 8 * c.nsoc) Bs[bl.sp + k] = reinterpret_cast<const double*>(c.sp)[k];
+    FOR_T(j, n) Bs[bl.xh + j] = c.x[j] / tau;
+    if (threadIdx.x == 0) {
+      Bs[bl.sc + 0] = fs.ea;
+      Bs[bl.sc + 1] = fs.ep;
+      Bs[bl.sc + 2] = (double)status;
+      Bs[bl.sc + 3] = tau;
+    }
+  }
   double nr2[2] = {0.0, 0.0};
   FOR_T(j, n) nr2[0] += c.rx[j] * c.rx[j];
   FOR_T(r, m) nr2[1] += c.rz[r] * c.rz[r];
@@ -1127,6 +1153,52 @@ __device__ __noinline__ void solveInstance(Ctx& c, const LaunchArgs& a, int inst
 // ------------------------------------------------------------------------------------------
 // kernel: persistent CTAs over an atomic instance queue
 // ------------------------------------------------------------------------------------------
+// Points the per-instance context at shared memory, the CTA's scratch and the pools (thread 0).
+__device__ void setupCtx(Ctx& c, const LaunchArgs& a, int inst, unsigned char* smem, double* scratch, int* sRedi) {
+  const SmemLayout& L = a.lay;
+  const InstanceDesc& D = a.desc[inst];
+  c.D = &D;
+  c.n = D.n; c.m = D.m; c.p = D.p; c.l = D.l; c.nsoc = D.nsoc; c.nr = D.nr; c.nUnits = D.nUnits;
+  const int* I = a.ipool;
+  c.psRow = I + D.iPsRow; c.psCol = I + D.iPsCol; c.pdiag = I + D.iPdiag;
+  c.plowIdx = I + D.iPlowIdx; c.plowSrc = I + D.iPlowSrc;
+  c.ap = I + D.iAp; c.ai = I + D.iAi;
+  c.arRow = I + D.iArRow; c.arCol = I + D.iArCol; c.arSrc = I + D.iArSrc;
+  c.azIdx = I + D.iAZIdx; c.azSrc = I + D.iAZSrc;
+  c.socOff = I + D.iSocOff; c.socDim = I + D.iSocDim;
+  c.unitAd = I + D.iUnitAd; c.unitSup = I + D.iUnitSup;
+  c.tgtIdx = I + D.iTgtIdx; c.tgtBeg = I + D.iTgtBeg; c.contrib = I + D.iContrib;
+  // scratch carve-up for this instance (scaled P in user order, then its CSR-order copy)
+  c.Pu = scratch + D.sPv;
+  c.Pv = c.Pu + D.nnzPu;
+  c.Av = scratch + D.sAv;
+  c.Ad = scratch + D.sAd;
+  c.T = scratch + D.sT;
+  c.qs = scratch + D.sQ;
+  c.bs = scratch + D.sB;
+  c.root64 = L.root64InSmem ? reinterpret_cast<double*>(smem + L.rootOff) : scratch + D.sRoot64;
+  // vectors: shared memory or scratch
+  double* vb = L.vecInSmem ? reinterpret_cast<double*>(smem + L.vecOff) : scratch + D.sVec;
+  const int nM = L.nMax, mM = L.mMax, NM = L.nMax + L.mMax, rM = rootTiles(L.nrMax) * kTile;
+  double* q = vb;
+  auto take = [&](int len) { double* r = q; q += (len + 1) & ~1; return r; };
+  c.x = take(nM); c.rx = take(nM); c.x1 = take(nM); c.Px1 = take(nM); c.dx = take(nM); c.tn = take(nM);
+  c.s = take(mM); c.z = take(mM); c.rz = take(mM); c.z1 = take(mM); c.dz = take(mM); c.ds = take(mM);
+  c.dcon = take(mM); c.lam = take(mM); c.tm = take(mM); c.tm2 = take(mM); c.cw = take(mM); c.cu = take(mM);
+  c.ev = take(mM);
+  c.rhs = take(NM); c.sol = take(NM); c.res = take(NM); c.cor = take(NM);
+  c.rr = take(rM);
+  c.sp = reinterpret_cast<SocScale*>(take(8 * L.nsocMax));
+  (void)take(rM);  // spare root-length vector (kept for the layout count)
+  c.root = L.rootInSmem ? reinterpret_cast<void*>(smem + L.rootOff) : reinterpret_cast<void*>(c.root64);
+  c.red = reinterpret_cast<double*>(smem + L.redOff);
+  c.sc = c.red + 128;
+  c.redi = sRedi;
+}
+
+// ------------------------------------------------------------------------------------------
+// kernel: persistent CTAs over an atomic instance queue
+// ------------------------------------------------------------------------------------------
 template <typename FT>
 __global__ void __launch_bounds__(512) ipmKernel(LaunchArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
@@ -1134,7 +1206,6 @@ __global__ void __launch_bounds__(512) ipmKernel(LaunchArgs a) {
   __shared__ int sRedi[4];
   __shared__ Ctx c;
   double* scratch = a.scratch + (int64_t)blockIdx.x * a.scratchStride;
-  const SmemLayout& L = a.lay;
   for (;;) {
     if (threadIdx.x == 0) sInst = atomicAdd(a.counter, 1);
     __syncthreads();
@@ -1142,49 +1213,98 @@ __global__ void __launch_bounds__(512) ipmKernel(LaunchArgs a) {
     __syncthreads();
     if (slot >= a.count) break;
     const int inst = a.order[slot];
-    if (threadIdx.x == 0) {
-    const InstanceDesc& D = a.desc[inst];
-    c.D = &D;
-    c.n = D.n; c.m = D.m; c.p = D.p; c.l = D.l; c.nsoc = D.nsoc; c.nr = D.nr; c.nUnits = D.nUnits;
-    const int* I = a.ipool;
-    c.psRow = I + D.iPsRow; c.psCol = I + D.iPsCol; c.pdiag = I + D.iPdiag;
-    c.plowIdx = I + D.iPlowIdx; c.plowSrc = I + D.iPlowSrc;
-    c.ap = I + D.iAp; c.ai = I + D.iAi;
-    c.arRow = I + D.iArRow; c.arCol = I + D.iArCol; c.arSrc = I + D.iArSrc;
-    c.azIdx = I + D.iAZIdx; c.azSrc = I + D.iAZSrc;
-    c.socOff = I + D.iSocOff; c.socDim = I + D.iSocDim;
-    c.unitAd = I + D.iUnitAd; c.unitSup = I + D.iUnitSup;
-    c.tgtIdx = I + D.iTgtIdx; c.tgtBeg = I + D.iTgtBeg; c.contrib = I + D.iContrib;
-    // scratch carve-up for this instance
-    c.Pu = scratch + D.sPv;  // Pu then Pv share the region start (see host layout)
-    c.Pv = c.Pu + D.nnzPu;
-    c.Av = scratch + D.sAv;
-    c.Ad = scratch + D.sAd;
-    c.T = scratch + D.sT;
-    c.qs = scratch + D.sQ;
-    c.bs = scratch + D.sB;
-    c.root64 = L.root64InSmem ? reinterpret_cast<double*>(smem + L.rootOff) : scratch + D.sRoot64;
-    // vectors: shared memory or scratch
-    double* vb = L.vecInSmem ? reinterpret_cast<double*>(smem + L.vecOff) : scratch + D.sVec;
-    const int nM = L.nMax, mM = L.mMax, NM = L.nMax + L.mMax, rM = rootTiles(L.nrMax) * kTile;
-    double* q = vb;
-    auto take = [&](int len) { double* r = q; q += (len + 1) & ~1; return r; };
-    c.x = take(nM); c.rx = take(nM); c.x1 = take(nM); c.Px1 = take(nM); c.dx = take(nM); c.tn = take(nM);
-    c.s = take(mM); c.z = take(mM); c.rz = take(mM); c.z1 = take(mM); c.dz = take(mM); c.ds = take(mM);
-    c.dcon = take(mM); c.lam = take(mM); c.tm = take(mM); c.tm2 = take(mM); c.cw = take(mM); c.cu = take(mM); c.ev = take(mM);
-    c.rhs = take(NM); c.sol = take(NM); c.res = take(NM); c.cor = take(NM);
-    c.rr = take(rM);
-    c.sp = reinterpret_cast<SocScale*>(take(8 * L.nsocMax));
-    (void)take(rM);  // spare root-length vector (kept for the layout count)
-    c.root = L.rootInSmem ? reinterpret_cast<void*>(smem + L.rootOff) : reinterpret_cast<void*>(c.root64);
-    c.red = reinterpret_cast<double*>(smem + L.redOff);
-    c.sc = c.red + 128;
-    c.redi = sRedi;
-    }
+    if (threadIdx.x == 0) setupCtx(c, a, inst, smem, scratch, sRedi);
     __syncthreads();
     loadInstance(c, a);
     solveInstance<FT>(c, a, inst);
   }
+}
+
+// ------------------------------------------------------------------------------------------
+// adjoint (new; no reference counterpart): differentiate the KKT conditions at the solution
+// with one extra solve through the saved final factorisation,
+//   K [u; v] = [D dL/dx; 0],  dL/dq = -u, dL/db = v, dL/dP = -(u x' + x u'), dL/dA = -(z u' + v x'),
+// all in the equilibrated space and mapped back through D, E, c (P^ = c D P D, q^ = c D q,
+// A^ = E A D, b^ = E b, x = D x^).
+// ------------------------------------------------------------------------------------------
+__device__ __noinline__ void adjointInstance(Ctx& c, const LaunchArgs& a) {
+  const InstanceDesc& D = *c.D;
+  const double* Bs = a.bwd + D.bwdOff;
+  const BwdLayout bl = bwdLayout(c.nr, c.n, c.m, c.nsoc);
+  const int n = c.n, m = c.m;
+  const int status = (int)Bs[bl.sc + 2];
+  if (threadIdx.x < SC_COUNT) c.sc[threadIdx.x] = 0.0;
+  FOR_T(r, m) {
+    c.cw[r] = Bs[bl.cw + r];
+    c.cu[r] = Bs[bl.cu + r];
+  }
+  FOR_T(k, 8 * c.nsoc) reinterpret_cast<double*>(c.sp)[k] = Bs[bl.sp + k];
+  if (a.lay.root64InSmem) {
+    const int64_t rs = rootSize(c.nr);
+    for (int64_t t = threadIdx.x; t < rs; t += blockDim.x) c.root64[t] = Bs[bl.root + t];
+  } else if (threadIdx.x == 0) {
+    c.root64 = const_cast<double*>(Bs + bl.root);
+  }
+  const double* dvec = a.dpool + D.dD;
+  const double* evec = a.dpool + D.dE;
+  const double cs = D.cscale;
+  FOR_T(j, n) c.rhs[j] = dvec[j] * a.gx[D.vX + j];
+  FOR_T(r, m) c.rhs[n + r] = 0.0;
+  __syncthreads();
+  const bool ok = status == 1;
+  if (ok) {
+    FactState fs{1, Bs[bl.sc + 1], Bs[bl.sc + 0]};
+    kktSolve<double>(c, a.st, fs, c.rhs, c.sol);
+  }
+  const double* u = c.sol;
+  const double* v = c.sol + n;
+  const double* xh = Bs + bl.xh;
+  const double* zh = Bs + bl.zh;
+  const int* Pp = a.ipool + D.iPp;
+  const int* Pi = a.ipool + D.iPi;
+  FOR_T(j, n) {
+    a.gq[D.vQ + j] = ok ? -u[j] * (cs * dvec[j]) : 0.0;
+    for (int k = Pp[j]; k < Pp[j + 1]; ++k) {
+      const int r = Pi[k];
+      double g = 0.0;
+      if (ok && r == j) g = -u[r] * xh[r];
+      else if (ok && r < j) g = -(u[r] * xh[j] + u[j] * xh[r]);
+      a.gP[D.vPx + k] = g * (cs * dvec[r] * dvec[j]);
+    }
+    for (int k = c.ap[j]; k < c.ap[j + 1]; ++k) {
+      const int r = c.ai[k];
+      a.gA[D.vAx + k] = ok ? -(zh[r] * u[j] + v[r] * xh[j]) * (evec[r] * dvec[j]) : 0.0;
+    }
+  }
+  FOR_T(r, m) a.gb[D.vB + r] = ok ? v[r] * evec[r] : 0.0;
+  __syncthreads();
+}
+
+__global__ void __launch_bounds__(512) adjointKernel(LaunchArgs a) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ int sInst;
+  __shared__ int sRedi[4];
+  __shared__ Ctx c;
+  double* scratch = a.scratch + (int64_t)blockIdx.x * a.scratchStride;
+  for (;;) {
+    if (threadIdx.x == 0) sInst = atomicAdd(a.counter, 1);
+    __syncthreads();
+    const int slot = sInst;
+    __syncthreads();
+    if (slot >= a.count) break;
+    const int inst = a.order[slot];
+    if (threadIdx.x == 0) setupCtx(c, a, inst, smem, scratch, sRedi);
+    __syncthreads();
+    loadInstance(c, a);
+    adjointInstance(c, a);
+  }
+}
+
+cudaError_t launchAdjoint(const LaunchArgs& a, int grid, int block, size_t smem, cudaStream_t stream) {
+  cudaError_t e = cudaFuncSetAttribute(adjointKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  adjointKernel<<<grid, block, smem, stream>>>(a);
+  return cudaGetLastError();
 }
 
 // explicit instantiations through the host launchers

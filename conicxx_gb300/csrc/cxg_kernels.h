@@ -42,6 +42,12 @@ struct LaunchArgs {
   double* warmS;
   double* warmZ;
   unsigned char* haveWarm;
+  double* bwd;            // saved final states (differentiable), or null
+  const double* gx;       // adjoint input dL/dx (concatenated, user units)
+  double* gq;             // adjoint outputs: dL/dq, dL/db, dL/d(P values), dL/d(A values)
+  double* gb;
+  double* gP;
+  double* gA;
   double* scratch;        // gridDim.x * scratchStride doubles
   int64_t scratchStride;
   DevSettings st;
@@ -49,6 +55,9 @@ struct LaunchArgs {
 };
 
 cudaError_t launchIpm(const LaunchArgs& a, int grid, int block, size_t smem, bool fp32, cudaStream_t stream);
+// One adjoint solve per instance with the saved final factorisation (same launch shape as the
+// forward groups).
+cudaError_t launchAdjoint(const LaunchArgs& a, int grid, int block, size_t smem, cudaStream_t stream);
 // Resident CTAs per SM of the IPM kernel for a block size and dynamic shared-memory size.
 cudaError_t ipmOccupancy(int* blocksPerSM, int block, size_t smem, bool fp32);
 

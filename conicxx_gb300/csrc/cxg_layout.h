@@ -85,8 +85,29 @@ struct InstanceDesc {
   int64_t sRoot64;                    // FP64 root (fallback / FP64 precision when not in SMEM)
   int64_t sVec;                       // FP64 vectors that do not fit in shared memory
   int64_t scratchDoubles;             // total per-CTA scratch this instance needs
+  int64_t bwdOff;                     // offset of this instance's saved final state (differentiable)
   double cost;                        // scheduling weight (~ nr^3)
 };
+
+// Saved final state of one instance for the adjoint (differentiable batches), in doubles:
+// FP64 root factor, NN/SOC scaling (w, G eigenvalues / u, SOC parameters), normalised iterate
+// x/tau and z/tau, and [bump_a, bump_p, status, tau].
+struct BwdLayout {
+  int64_t root, cw, cu, sp, xh, zh, sc, total;
+};
+CXG_HD BwdLayout bwdLayout(int nr, int n, int m, int nsoc) {
+  BwdLayout b{};
+  int64_t o = 0;
+  b.root = o; o += rootSize(nr);
+  b.cw = o; o += m;
+  b.cu = o; o += m;
+  b.sp = o; o += 8 * (int64_t)nsoc;
+  b.xh = o; o += n;
+  b.zh = o; o += m;
+  b.sc = o; o += 4;
+  b.total = (o + 1) & ~int64_t(1);
+  return b;
+}
 
 // Kernel-side copy of the solver settings (cxg_settings) in the units the kernel uses.
 struct DevSettings {

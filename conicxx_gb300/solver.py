@@ -61,6 +61,7 @@ class Solver:
             self._h = None
 
     def setup(self, qp: QP, settings: Settings = None, **kw) -> bool:
+        kw.setdefault("differentiable", 1)
         st = _settings(settings, _abi.PRECISION_FP64, **kw)
         prob, keep = make_problem_struct(qp)
         rc = lib().cxg_solver_setup(self._h, C.byref(prob), C.byref(st))
@@ -189,6 +190,20 @@ class BatchSolver:
         check(lib().cxg_batch_solve(self._h, dptr(x), dptr(s), dptr(z),
                                     infos.ctypes.data_as(C.POINTER(Info))), "cxg_batch_solve")
         return x, s, z, infos
+
+    def backward(self, dl_dx):
+        """Adjoint of every instance at its last solution (needs differentiable=1): returns the
+        concatenated (dL/dq, dL/db, dL/d(P values), dL/d(A values))."""
+        g = np.ascontiguousarray(dl_dx, dtype=np.float64)
+        dq, db = np.zeros(self.n_total), np.zeros(self.m_total)
+        dP, dA = np.zeros(self.nnzP), np.zeros(self.nnzA)
+        check(lib().cxg_batch_backward(self._h, dptr(g), dptr(dq), dptr(db), dptr(dP), dptr(dA)),
+              "cxg_batch_backward")
+        return dq, db, dP, dA
+
+    def backward_device(self, gx_ptr, dq_ptr, db_ptr, dP_ptr, dA_ptr, stream_ptr):
+        check(lib().cxg_batch_backward_device(self._h, gx_ptr, dq_ptr, db_ptr, dP_ptr, dA_ptr, stream_ptr),
+              "cxg_batch_backward_device")
 
     def solve_device(self, x_ptr, s_ptr, z_ptr, stream_ptr, infos=None):
         """Enqueue a solve writing device buffers (raw pointers) on a CUDA stream handle."""

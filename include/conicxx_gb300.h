@@ -91,6 +91,8 @@ typedef struct cxg_settings {
   double mixed_fallback_tol;  /* relative KKT residual above which an FP32-factor solve is redone
                                  with an FP64 factor (default 1e-10) */
   int threads_per_instance;   /* 0 = autotuned; else 64/128/256/512 */
+  int differentiable;         /* keep each instance's final factorisation, scaling and iterate on the
+                                 device so backward() can reuse them (default 0; cxg_solver: 1) */
 } cxg_settings;
 
 /* conicxx::Info (include/conicxx/solution.h:18-26) plus Solution::objective/status and counters. */

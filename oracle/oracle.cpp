@@ -1299,6 +1299,46 @@ class Solver {
     info.mu = mu();
   }
 
+  // Adjoint of the KKT conditions at the last solution (new; no reference counterpart): one
+  // extra KKT solve with the final factorisation and NT scaling,
+  //   K [u; v] = [D dL/dx; 0]   (equilibrated space),
+  // then dL/dq = -u, dL/db = v, dL/dP = -(u x' + x u'), dL/dA = -(z u' + v x'), mapped back
+  // through the equilibration (x = D xh, P^ = c D P D, q^ = c D q, A^ = E A D, b^ = E b).
+  bool adjoint(const double* dldx, double* dq, double* db, double* dPx, double* dAx) {
+    if (status != CXG_STATUS_SOLVED) return false;
+    const double* d = eq.d.data();
+    const double* e = eq.e.data();
+    const double cs = eq.c;
+    Vec rhs((size_t)(n + m), 0.0), sol;
+    for (int j = 0; j < n; ++j) rhs[(size_t)j] = d[j] * dldx[j];
+    kkt.solve(rhs, sol);
+    const double* u = sol.data();
+    const double* v = sol.data() + n;
+    Vec xh((size_t)n), zh((size_t)m);
+    for (int j = 0; j < n; ++j) xh[(size_t)j] = x[(size_t)j] / tau;
+    for (int r = 0; r < m; ++r) zh[(size_t)r] = z[(size_t)r] / tau;
+    if (dq) for (int j = 0; j < n; ++j) dq[j] = -u[j] * (cs * d[j]);
+    if (db) for (int r = 0; r < m; ++r) db[r] = v[r] * e[r];
+    if (dPx) {
+      for (int col = 0; col < P.cols; ++col)
+        for (int k = P.p[(size_t)col]; k < P.p[(size_t)col + 1]; ++k) {
+          const int r = P.i[(size_t)k];
+          double g = 0.0;
+          if (r == col) g = -u[r] * xh[(size_t)r];
+          else if (r < col) g = -(u[r] * xh[(size_t)col] + u[col] * xh[(size_t)r]);
+          dPx[k] = g * (cs * d[r] * d[col]);
+        }
+    }
+    if (dAx) {
+      for (int col = 0; col < A.cols; ++col)
+        for (int k = A.p[(size_t)col]; k < A.p[(size_t)col + 1]; ++k) {
+          const int r = A.i[(size_t)k];
+          dAx[k] = -(zh[(size_t)r] * u[col] + v[r] * xh[(size_t)col]) * (e[r] * d[col]);
+        }
+    }
+    return true;
+  }
+
   void solve() {
     info = cxg_info{};
     trace.clear();
@@ -1450,6 +1490,10 @@ int orc_solve(void* h, double* x, double* s, double* z, cxg_info* info) {
   if (z && !S->solz.empty()) std::memcpy(z, S->solz.data(), sizeof(double) * S->solz.size());
   if (info) *info = S->info;
   return S->status;
+}
+
+int orc_adjoint(void* h, const double* dldx, double* dq, double* db, double* dPx, double* dAx) {
+  return static_cast<orc::Solver*>(h)->adjoint(dldx, dq, db, dPx, dAx) ? 1 : 0;
 }
 
 int orc_trace_len(void* h) { return (int)static_cast<orc::Solver*>(h)->trace.size(); }

@@ -39,6 +39,7 @@ def lib():
         L.orc_update.argtypes = [vp, ip, ip, dp, dp, ip, ip, dp, dp]
         L.orc_set_warm_start.argtypes = [vp, dp, dp, dp]
         L.orc_solve.argtypes = [vp, dp, dp, dp, C.POINTER(Info)]
+        L.orc_adjoint.argtypes = [vp, dp, dp, dp, dp, dp]
         L.orc_trace_len.argtypes = [vp]
         L.orc_trace.argtypes = [vp, dp]
         L.orc_equilibration.argtypes = [vp, dp, dp, dp]
@@ -124,6 +125,15 @@ class OracleSolver:
         if k:
             L.orc_trace(self._h, dptr(out))
         return out
+
+    def adjoint(self, dl_dx):
+        """FP64 adjoint at the last Solved solution: (dL/dq, dL/db, dL/dPx, dL/dAx)."""
+        qp = self.qp
+        g = np.ascontiguousarray(dl_dx, dtype=np.float64)
+        dq, db, dP, dA = np.zeros(qp.n), np.zeros(qp.m), np.zeros(qp.P.nnz), np.zeros(qp.A.nnz)
+        if not lib().orc_adjoint(self._h, dptr(g), dptr(dq), dptr(db), dptr(dP), dptr(dA)):
+            raise ValueError("adjoint needs a Solved solution")
+        return dq, db, dP, dA
 
     def equilibration(self):
         d, e, c = np.zeros(self.qp.n), np.zeros(self.qp.m), C.c_double()

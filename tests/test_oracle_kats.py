@@ -222,3 +222,19 @@ def test_golden_instances_reproduce(oracle_mod, golden_instances):
         x, s, z, info, _ = oracle_mod.solve(qp)
         assert info["status"] == exp["status"] and info["iterations"] == exp["iterations"], name
         assert rel(x, exp["x"]) < 1e-9, name
+
+
+def test_oracle_adjoint_closed_form(oracle_mod, kats):
+    """The FP64 adjoint (new; no reference counterpart) on the equality QP of
+    test/solver/test_solve_qp.cpp:9-34, whose solution map is affine: x = -q + (b+q0+q1)/2 (1,1)."""
+    qp = kat_qp(kats[0])
+    S = oracle_mod.OracleSolver()
+    assert S.setup(qp)
+    x, s, z, info = S.solve()
+    t = np.array([0.3, -1.2])
+    g = x - t
+    dq, db, dP, dA = S.adjoint(g)
+    J = -np.eye(2) + 0.5 * np.ones((2, 2))
+    assert np.allclose(dq, J @ g, atol=1e-7) and np.allclose(db, [0.5 * g.sum()], atol=1e-7)
+    # dL/dP (upper diagonal entries): -(u_i x_i) with u = -dq
+    assert np.allclose(dP, -(-dq) * x, atol=1e-7)
