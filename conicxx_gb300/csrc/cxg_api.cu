@@ -12,6 +12,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <numeric>
 #include <string>
 #include <vector>
@@ -858,4 +859,104 @@ extern "C" int cxg_batch_backward_device(cxg_batch* B, const double* dL_dx, doub
   if (!dL_dx) return setErr(CXG_E_INVALID, "null dL/dx");
   return enqueueAdjoint(B, (cudaStream_t)stream, dL_dx, dq ? dq : B->dGq, db ? db : B->dGb, dPx ? dPx : B->dGP,
                         dAx ? dAx : B->dGA);
+}
+
+// ------------------------------------------------------------------------------------------
+// allocation-free solve (no reference counterpart)
+// ------------------------------------------------------------------------------------------
+// Some callers cannot allocate or free device memory while they solve. An example is a
+// simulator's per-timestep loop that reserved its memory up front: there an allocation may fail
+// mid-step and cudaFree synchronises the device. For them the IPM kernel's per-CTA working memory
+// comes from this fixed array instead of the batch's own scratch.
+//
+// Layout: the first kNoallocCounterBytes hold the work-queue counters (one int per size bucket).
+// These must be zero when a launch starts, so every call clears them on its stream. The rest is
+// the per-CTA FP64 scratch. The kernel writes scratch before it reads it, so no clearing is needed.
+static __device__ __align__(256) unsigned char g_noallocArena[CXG_NOALLOC_SCRATCH_BYTES];
+constexpr int64_t kNoallocCounterBytes = 256;
+constexpr int kNoallocMaxDevices = 64;
+static unsigned char* g_noallocPtr[kNoallocMaxDevices];
+static std::mutex g_noallocMutex;
+
+// Address of the array on the current device `dev`. It is looked up once per device, on the first
+// call with that device current; that lookup loads this module if it is not loaded yet.
+static int noallocArena(int dev, unsigned char** out) {
+  if (dev < 0 || dev >= kNoallocMaxDevices) return setErr(CXG_E_UNSUPPORTED, "device index beyond 63");
+  std::lock_guard<std::mutex> lock(g_noallocMutex);
+  if (!g_noallocPtr[dev]) {
+    unsigned char* ptr = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress((void**)&ptr, g_noallocArena);
+    if (e != cudaSuccess || !ptr)
+      return setErr(CXG_E_CUDA, std::string("cudaGetSymbolAddress(fixed scratch): ") + cudaGetErrorString(e));
+    g_noallocPtr[dev] = ptr;
+  }
+  *out = g_noallocPtr[dev];
+  return CXG_OK;
+}
+
+extern "C" int cxg_batch_solve_device_noalloc(cxg_batch* B, double* x, double* s, double* z, cxg_info* info,
+                                              void* stream) {
+  if (!B) return setErr(CXG_E_INVALID, "null batch");
+  int dev = -1;
+  CX_CUDA(cudaGetDevice(&dev));
+  if (dev != B->device) return setErr(CXG_E_INVALID, "the batch lives on another device: make that device current");
+  const size_t G = B->groups.size();
+  if ((int64_t)(G * sizeof(int)) > kNoallocCounterBytes) return setErr(CXG_E_INTERNAL, "too many size buckets");
+  const int64_t capDoubles = (CXG_NOALLOC_SCRATCH_BYTES - kNoallocCounterBytes) / (int64_t)sizeof(double);
+  for (const Group& g : B->groups)
+    if (g.stride > capDoubles) {
+      char msg[256];
+      std::snprintf(msg, sizeof(msg),
+                    "an instance of this batch needs %lld bytes of working memory per CTA (bucket nr <= %d); "
+                    "the fixed scratch holds %lld",
+                    (long long)(g.stride * 8), g.lay.nrMax, (long long)(capDoubles * 8));
+      return setErr(CXG_E_UNSUPPORTED, msg);
+    }
+  unsigned char* arena = nullptr;
+  int rc = noallocArena(dev, &arena);
+  if (rc) return rc;
+  int* counters = (int*)arena;
+  double* scratch = (double*)(arena + kNoallocCounterBytes);
+  cudaStream_t st = (cudaStream_t)stream;
+  CX_CUDA(cudaMemsetAsync(counters, 0, (size_t)kNoallocCounterBytes, st));
+  const DevSettings ds = makeDevSettings(B->st, B->kktSt);
+  // Buckets run in stream order, so each may use the whole scratch from its start.
+  for (size_t gi = 0; gi < G; ++gi) {
+    const Group& g = B->groups[gi];
+    LaunchArgs a{};
+    a.desc = B->dDesc;
+    a.order = B->dOrder + g.begin;
+    a.count = g.count;
+    a.counter = counters + gi;
+    a.ipool = B->dIpool;
+    a.dpool = B->dDpool;
+    a.Px = B->dPx;
+    a.q = B->dq;
+    a.Ax = B->dAx;
+    a.b = B->db;
+    a.x = B->dx;
+    a.s = B->ds;
+    a.z = B->dz;
+    a.results = B->dRes;
+    a.warmX = B->dWx;
+    a.warmS = B->dWs;
+    a.warmZ = B->dWz;
+    a.haveWarm = B->dHaveWarm;
+    a.bwd = B->dBwd;
+    a.scratch = scratch;
+    a.scratchStride = g.stride;
+    a.st = ds;
+    a.lay = g.lay;
+    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(g.grid, capDoubles / g.stride));
+    CX_CUDA(launchIpm(a, grid, g.block, g.smem, g.fp32, st));
+  }
+  B->lastLaunches = (int)G;
+  if (x && B->pools.totQ) CX_CUDA(cudaMemcpyAsync(x, B->dx, (size_t)B->pools.totQ * 8, cudaMemcpyDeviceToDevice, st));
+  if (s && B->pools.totB) CX_CUDA(cudaMemcpyAsync(s, B->ds, (size_t)B->pools.totB * 8, cudaMemcpyDeviceToDevice, st));
+  if (z && B->pools.totB) CX_CUDA(cudaMemcpyAsync(z, B->dz, (size_t)B->pools.totB * 8, cudaMemcpyDeviceToDevice, st));
+  if (info) {
+    CX_CUDA(cudaStreamSynchronize(st));
+    return fetchInfo(B, info, 0.0);
+  }
+  return CXG_OK;
 }

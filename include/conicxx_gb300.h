@@ -193,6 +193,31 @@ int cxg_batch_backward(cxg_batch* batch, const double* dL_dx, double* dq, double
                        double* dAx);
 int cxg_batch_backward_device(cxg_batch* batch, const double* dL_dx, double* dq, double* db,
                               double* dPx, double* dAx, void* stream);
+/* Allocation-free solve. No reference counterpart: ConicXX has no device path. It exists for
+ * callers that must not allocate or free device memory while they solve. One example is a
+ * simulator's per-timestep loop that reserves its device memory up front. There, an allocation
+ * could fail in mid-step, and cudaFree would synchronise the whole device.
+ *
+ * Same contract as cxg_batch_solve_device, with three differences:
+ * - The IPM kernel's per-CTA working memory comes from one fixed device array of
+ *   CXG_NOALLOC_SCRATCH_BYTES per device, not from memory the batch owns.
+ * - The size buckets run one after another on `stream`, with no captured graph and no stream or
+ *   event creation.
+ * - Each bucket's persistent grid is cut down to what the array holds.
+ *
+ * The call allocates nothing. The first call on a device looks up that array's address with the
+ * device current. Make that first call before any stream capture.
+ *
+ * Returns CXG_E_UNSUPPORTED with a message if one CTA's working memory for a bucket exceeds the
+ * array, that is, if one instance's plan is too big.
+ *
+ * The work-queue counters live in the same array; each call clears them on `stream` before its
+ * launches. Calls whose work overlaps in time share the array and race: two in flight at once
+ * on one device, from any batch and on any stream, corrupt each other's results. Keep them
+ * ordered on one stream or synchronise between them. */
+#define CXG_NOALLOC_SCRATCH_BYTES (32ll << 20)
+int cxg_batch_solve_device_noalloc(cxg_batch* batch, double* x, double* s, double* z, cxg_info* info,
+                                   void* stream);
 /* Kernel launches enqueued by the last solve/backward call of this batch. */
 int cxg_batch_last_launches(const cxg_batch* batch);
 /* Device footprint of the batch in bytes: index plans + equilibration (plan), problem values +
