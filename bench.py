@@ -4,7 +4,7 @@ Workload (one step): 4096 independent friction-contact QPs, c ~ U{4..64} contact
 (n = 3c forces, m = 4c cone rows: R^c_+ x c Q^3), solved to the 1e-8 relative gap by one
 batched mixed-precision (FP32 factor, FP64 refinement) launch sequence. Synthetic, seeded data
 of the reference's contact-problem shape; cold starts (warm_start off) so every step repeats
-the full solve. Inputs stay resident in HBM (they exceed the 129 MB L2, so no flush is needed).
+the full solve. Inputs stay resident in HBM; the L2 is flushed (256 MB write) between timed steps.
 
   value  -- solves/s of the device-resident batch (CUDA events on the solver's stream)
   e2e    -- the same through the C-ABI with pinned HOST buffers: H2D of the step's values,
@@ -32,8 +32,15 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "QP solves/s at 1e-8 rel. gap: batched mixed-prec vs plain GPU vs host CPU; fwd+bwd µs"
-WORKLOAD = "batched friction-contact QPs: 4096 instances, c~U{4..64}, n=3c, cones R^c_+ x c Q^3, mixed FP32/FP64"
 COUNT = 4096
+
+
+def workload(count):
+    return (f"batched friction-contact QPs: {count} instances, c~U{{4..64}}, n=3c, cones R^c_+ x c Q^3, "
+            "mixed FP32/FP64")
+
+
+WORKLOAD = workload(COUNT)
 
 
 def dist_env():
@@ -113,7 +120,8 @@ def run_gb300(args, rank, world, local_rank):
         import torch.distributed as dist
 
         dist.init_process_group("nccl")
-    qps = generators.contact_batch(COUNT, base_seed=rank * COUNT)
+    count = args.count
+    qps = generators.contact_batch(count, base_seed=rank * count)
     st = default_settings(precision=1, warm_start=0)
     t0 = time.perf_counter()
     B = BatchSolver(qps, settings=st)
@@ -126,9 +134,17 @@ def run_gb300(args, rank, world, local_rank):
     stream = torch.cuda.Stream(device=dev)
     sp = stream.cuda_stream
 
-    def step():
+    def solve_step():
+        if args.entry == "noalloc":
+            B.solve_device_noalloc(int(dx.data_ptr()), int(ds.data_ptr()), int(dz.data_ptr()), sp)
+        else:
+            B.solve_device(int(dx.data_ptr()), int(ds.data_ptr()), int(dz.data_ptr()), sp)
+
+    def step(ev=None):
         B.update_values_device(*(int(t.data_ptr()) for t in dvals), sp)
-        B.solve_device(int(dx.data_ptr()), int(ds.data_ptr()), int(dz.data_ptr()), sp)
+        if ev is not None:
+            ev.record(stream)
+        solve_step()
 
     with torch.cuda.stream(stream):
         for _ in range(args.warmup):
@@ -142,22 +158,25 @@ def run_gb300(args, rank, world, local_rank):
 
             dist.barrier()
 
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
     sampler = ClockSampler(local_rank)
     sampler.start()
-    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    evs = [tuple(torch.cuda.Event(enable_timing=True) for _ in range(3)) for _ in range(args.steps)]
     barrier()
     torch.cuda.synchronize()
     w0 = time.perf_counter()
     with torch.cuda.stream(stream):
         for i in range(args.steps):
+            flush.fill_(i & 0xFF)  # evict the L2 between timed steps
             evs[i][0].record(stream)
-            step()
-            evs[i][1].record(stream)
+            step(evs[i][1])
+            evs[i][2].record(stream)
     torch.cuda.synchronize()
     barrier()
     wall = time.perf_counter() - w0
     clocks = sampler.stop()
-    step_ms = np.array([a.elapsed_time(b_) for a, b_ in evs])
+    step_ms = np.array([a.elapsed_time(c_) for a, _, c_ in evs])
+    ipm_ms = float(np.mean([b_.elapsed_time(c_) for _, b_, c_ in evs]))
     ms_local = float(step_ms.mean())
     ms = ms_local
     if world > 1:
@@ -166,13 +185,22 @@ def run_gb300(args, rank, world, local_rank):
         t = torch.tensor([ms_local], device=dev)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t.item())
-    infos = np.zeros(COUNT, dtype=INFO_DTYPE)
-    B.solve_device(int(dx.data_ptr()), int(ds.data_ptr()), int(dz.data_ptr()), sp, infos)
+    infos = np.zeros(count, dtype=INFO_DTYPE)
+    if args.entry == "noalloc":
+        B.solve_device_noalloc(int(dx.data_ptr()), int(ds.data_ptr()), int(dz.data_ptr()), sp, infos)
+    else:
+        B.solve_device(int(dx.data_ptr()), int(ds.data_ptr()), int(dz.data_ptr()), sp, infos)
     solved_frac = float(np.mean(infos["status"] == 1))
     statuses = {int(k): int(v) for k, v in zip(*np.unique(infos["status"], return_counts=True))}
 
     result = {}
-    if rank == 0:
+    if rank == 0 and args.legs == "main":
+        hbm_peak, peak_kind = peaks()
+        achieved = B.algorithmic_bytes() / (ipm_ms * 1e-3) / 1e9
+        result = dict(roofline={"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                                "frac": achieved / hbm_peak, "traffic": None, "peak_kind": peak_kind,
+                                "ipm_ms": ipm_ms})
+    elif rank == 0:
         # ---- e2e through the C-ABI with pinned host buffers ----
         pin = lambda a: torch.from_numpy(a).pin_memory().numpy()  # noqa: E731
         hvals = [pin(v) for v in (Px, q, Ax, b)]
@@ -260,27 +288,33 @@ def run_gb300(args, rank, world, local_rank):
         sample = qps[:args.cpu_sample]
         cpu_wall, cpu_st, _ = orc.batch_solve(sample, ncpu, warm_start=0)
         cpu_rate = len(sample) / cpu_wall
-        # ---- roofline of the IPM kernel (the only kernel of the timed region) ----
+        # ---- roofline of the IPM launch set (one persistent launch per size bucket, run
+        # concurrently; timed by CUDA events around the solve on the launching stream) ----
         hbm_peak, peak_kind = peaks()
         algo_bytes = B.algorithmic_bytes()
-        achieved = algo_bytes / (ms * 1e-3) / 1e9
-        traffic = None
+        achieved = algo_bytes / (ipm_ms * 1e-3) / 1e9
+        traffic, fp64_pipe = None, None
         tp = os.path.join(ROOT, "profiles", "ipm_kernel_traffic.json")
         if os.path.exists(tp):
             with open(tp) as f:
-                traffic = json.load(f).get("dram_bytes_per_launch_4096")
+                tj = json.load(f)
+            # DRAM bytes of the launch set scale with the number of instances
+            traffic = tj["dram_bytes_per_step"] * count / tj["instances"]
+            fp64_pipe = tj.get("fp64_pipe_active_frac")
         result = dict(
-            e2e={"value": COUNT / e2e_s, "unit": "solves/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+            e2e={"value": count / e2e_s, "unit": "solves/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
             plain_gpu={"value": plain_rate, "unit": "solves/s", "instances": plain_n, "precision": "fp64",
-                       "batched_over_plain": (COUNT / (ms * 1e-3)) / plain_rate},
+                       "batched_over_plain": (count / (ms * 1e-3)) / plain_rate},
             cpu_baseline={"value": cpu_rate, "unit": "solves/s", "cores": ncpu, "kind": "port",
-                          "sample": f"first {len(sample)} of the 4096 instances, one instance per thread, "
+                          "sample": f"first {len(sample)} of the {count} instances, one instance per thread, "
                                     f"cold start, FP64 oracle restatement of the reference",
                           "solved_fraction": float(np.mean(cpu_st == 1))},
             roofline={"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                       "frac": achieved / hbm_peak, "traffic": traffic, "peak_kind": peak_kind,
-                      "note": "IPM kernel; HBM bytes = problem data + plans + solutions per launch; the kernel "
-                              "is bound by the FP64 pipe and barrier latency, not HBM (see profiles/)"},
+                      "ipm_ms": ipm_ms, "algorithmic_bytes": algo_bytes, "fp64_pipe_active_frac": fp64_pipe,
+                      "note": "IPM launch set (one persistent launch per size bucket); algorithmic bytes = "
+                              "plans + problem values + solutions + results read/written once; the kernel is "
+                              "bound by FP64 pipe and barrier latency of the slowest instances, not by HBM"},
             fwd_bwd=fwd_bwd,
             setup_s=setup_s,
         )
@@ -328,6 +362,12 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-sample", type=int, default=1024)
     ap.add_argument("--plain-instances", type=int, default=16)
+    ap.add_argument("--count", type=int, default=COUNT, help="contact instances per GPU")
+    ap.add_argument("--entry", default="graph", choices=["graph", "noalloc"],
+                    help="graph: the captured concurrent-bucket solve (default); noalloc: the allocation-free "
+                         "entry point (direct launches, buckets in sequence)")
+    ap.add_argument("--legs", default="all", choices=["all", "main"],
+                    help="main: only the device-resident batched timing (profiling runs)")
     args = ap.parse_args()
     rank, world, local_rank = dist_env()
     if args.impl == "reference":
@@ -342,12 +382,13 @@ def main():
     ms, wall, clocks, launches, solved_frac, statuses, extra = run_gb300(args, rank, world, local_rank)
     if rank == 0:
         out = {
-            "metric": METRIC, "value": world * COUNT / (ms * 1e-3), "unit": "solves/s", "n_gpus": world,
+            "metric": METRIC, "value": world * args.count / (ms * 1e-3), "unit": "solves/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "mixed fp32-factor/fp64",
             "data": "synthetic (seeded contact generator)",
-            "config": {"workload": WORKLOAD, "count_per_gpu": COUNT, "parallelism": f"instances x{world}",
-                       "l2": "inputs resident in HBM exceed the 129 MB L2; no flush",
+            "config": {"workload": workload(args.count), "count_per_gpu": args.count, "entry": args.entry,
+                       "parallelism": f"instances x{world}",
+                       "l2": "flushed between timed steps (256 MB device write outside the step events)",
                        "solved_fraction": solved_frac, "statuses": statuses, "warm_start": False},
             "wall_s_timed_region": wall, "gpu_launches": launches * args.steps, "clocks": clocks,
         }

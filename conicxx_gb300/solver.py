@@ -211,6 +211,13 @@ class BatchSolver:
         check(lib().cxg_batch_solve_device(self._h, x_ptr, s_ptr, z_ptr, ip_, stream_ptr),
               "cxg_batch_solve_device")
 
+    def solve_device_noalloc(self, x_ptr, s_ptr, z_ptr, stream_ptr, infos=None):
+        """Like solve_device, through the allocation-free entry point (fixed device workspace,
+        buckets launched one after another on the stream, no graph)."""
+        ip_ = infos.ctypes.data_as(C.POINTER(Info)) if infos is not None else None
+        check(lib().cxg_batch_solve_device_noalloc(self._h, x_ptr, s_ptr, z_ptr, ip_, stream_ptr),
+              "cxg_batch_solve_device_noalloc")
+
     def update_values_device(self, Px_ptr, q_ptr, Ax_ptr, b_ptr, stream_ptr):
         check(lib().cxg_batch_update_values_device(self._h, Px_ptr, q_ptr, Ax_ptr, b_ptr, stream_ptr),
               "cxg_batch_update_values_device")
