@@ -95,6 +95,11 @@ class Info(C.Structure):
         ("time_factor_s", C.c_double),
         ("time_kkt_solve_s", C.c_double),
         ("time_other_s", C.c_double),
+        ("time_assemble_s", C.c_double),
+        ("time_ldlt_s", C.c_double),
+        ("time_dense_solve_s", C.c_double),
+        ("time_residual_s", C.c_double),
+        ("factor_attempts", C.c_int),
     ]
 
     def as_dict(self):

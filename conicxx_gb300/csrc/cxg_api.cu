@@ -199,11 +199,10 @@ static int64_t r2(int64_t v) { return (v + 1) & ~int64_t(1); }
 static const int kBucketEdges[] = {32, 64, 96, 128, 160, 192, 256, 384, 512, 1024, 2048, 4096};
 
 static int chooseBlock(int nrMax, int requested) {
-  if (requested == 64 || requested == 128 || requested == 256 || requested == 512) return requested;
+  if (requested == 64 || requested == 128 || requested == 256) return requested;
   if (nrMax <= 64) return 64;
   if (nrMax <= 128) return 128;
-  if (nrMax <= 512) return 256;
-  return 512;
+  return 256;
 }
 
 static int buildGroups(cxg_batch* B) {
@@ -292,6 +291,7 @@ static int buildGroups(cxg_batch* B) {
       D.sB = o; o += r2(D.m);
       D.sRoot64 = o; o += needRoot64 ? r2(rootSize(D.nr)) : 0;
       D.sVec = o; o += L.vecInSmem ? 0 : vecDoubles(L.nMax, L.mMax, L.nrMax, L.nsocMax);
+      D.sVecG = o; o += vecGlobalDoubles(L.mMax);
       D.scratchDoubles = o;
       stride = std::max(stride, o);
     }
@@ -585,10 +585,15 @@ static void resultToInfo(const DevResult& R, cxg_info& I, double setupTime, doub
   I.fp64_fallbacks = R.fp64_fallbacks;
   I.refine_steps = R.refine_steps;
   I.max_relres = R.max_relres;
+  I.factor_attempts = R.factor_attempts;
   if (g_clockHz > 0.0) {
     I.time_factor_s = (double)R.cycles[1] / g_clockHz;
     I.time_kkt_solve_s = (double)R.cycles[2] / g_clockHz;
     I.time_other_s = (double)R.cycles[3] / g_clockHz;
+    I.time_assemble_s = (double)R.cycles[4] / g_clockHz;
+    I.time_ldlt_s = (double)R.cycles[5] / g_clockHz;
+    I.time_dense_solve_s = (double)R.cycles[6] / g_clockHz;
+    I.time_residual_s = (double)R.cycles[7] / g_clockHz;
   }
 }
 

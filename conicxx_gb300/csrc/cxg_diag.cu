@@ -9,6 +9,7 @@
 
 #include "conicxx_gb300.h"
 #include "cxg_cones.cuh"
+#include "cxg_kernels.h"
 #include "cxg_plan.h"
 
 namespace cxg {
@@ -194,5 +195,59 @@ extern "C" int cxg_equilibration(const cxg_problem* pr, const cxg_settings* st, 
   if (d) std::memcpy(d, dv.data(), sizeof(double) * dv.size());
   if (e) std::memcpy(e, ev.data(), sizeof(double) * ev.size());
   if (c) *c = cv;
+  return CXG_OK;
+}
+
+extern "C" int cxg_dense_ldlt(int nr, int nx, const double* K, const double* b, int arith, int threads,
+                              int linear_solver, double* L, double* D, double* x, long long* cycles, int* flags) {
+  using namespace cxg;
+  if (nr < 1 || nx < 0 || nx > nr || !K || !b || arith < 0 || arith > 2 || threads < 32 || threads > 256 ||
+      (threads % 32) != 0) {
+    lastErrorRef() = "cxg_dense_ldlt: bad arguments";
+    return CXG_E_INVALID;
+  }
+  std::vector<void*> bufs;
+  int dev = 0, optin = 0;
+  DG_CUDA(cudaGetDevice(&dev));
+  DG_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  if (denseProbeSmem(arith, nr) + 2048 > (size_t)optin) {
+    lastErrorRef() = "cxg_dense_ldlt: matrix too large for one CTA's shared memory";
+    return CXG_E_UNSUPPORTED;
+  }
+  cxg_settings cs;
+  cxg_default_settings(&cs);
+  DevSettings st{};
+  st.dynamic_reg_eps = cs.dynamic_reg_eps;
+  st.dynamic_reg_delta = cs.dynamic_reg_delta;
+  st.linear_solver = linear_solver;
+  const size_t nn = (size_t)nr * (size_t)nr;
+  auto alloc = [&](size_t bytes) -> void* {
+    void* p = nullptr;
+    if (cudaMalloc(&p, bytes ? bytes : 8) != cudaSuccess) return nullptr;
+    bufs.push_back(p);
+    return p;
+  };
+  double* dK = (double*)alloc(nn * 8);
+  double* dB = (double*)alloc((size_t)nr * 8);
+  double* dL = (double*)alloc(nn * 8);
+  double* dD = (double*)alloc((size_t)nr * 8);
+  double* dX = (double*)alloc((size_t)nr * 8);
+  long long* dC = (long long*)alloc(2 * sizeof(long long));
+  int* dF = (int*)alloc(2 * sizeof(int));
+  if (bufs.size() != 7) {
+    for (void* p : bufs) cudaFree(p);
+    lastErrorRef() = "cxg_dense_ldlt: device allocation failed";
+    return CXG_E_NOMEM;
+  }
+  DG_CUDA(cudaMemcpy(dK, K, nn * 8, cudaMemcpyHostToDevice));
+  DG_CUDA(cudaMemcpy(dB, b, (size_t)nr * 8, cudaMemcpyHostToDevice));
+  DG_CUDA(launchDenseProbe(arith, nr, nx, dK, dB, st, threads, dL, dD, dX, dC, dF));
+  DG_CUDA(cudaDeviceSynchronize());
+  if (L) DG_CUDA(cudaMemcpy(L, dL, nn * 8, cudaMemcpyDeviceToHost));
+  if (D) DG_CUDA(cudaMemcpy(D, dD, (size_t)nr * 8, cudaMemcpyDeviceToHost));
+  if (x) DG_CUDA(cudaMemcpy(x, dX, (size_t)nr * 8, cudaMemcpyDeviceToHost));
+  if (cycles) DG_CUDA(cudaMemcpy(cycles, dC, 2 * sizeof(long long), cudaMemcpyDeviceToHost));
+  if (flags) DG_CUDA(cudaMemcpy(flags, dF, 2 * sizeof(int), cudaMemcpyDeviceToHost));
+  for (void* p : bufs) cudaFree(p);
   return CXG_OK;
 }

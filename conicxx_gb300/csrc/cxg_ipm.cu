@@ -14,6 +14,7 @@
 #include <stdint.h>
 
 #include "cxg_cones.cuh"
+#include "cxg_df64.cuh"
 #include "cxg_kernels.h"
 #include "cxg_layout.h"
 
@@ -97,7 +98,7 @@ enum {
 };
 
 // Phase cycle counters (record_timings), kept by thread 0 in the scalar area after PivotStats.
-enum { TM_FACTOR = 0, TM_SOLVE = 1 };
+enum { TM_FACTOR = 0, TM_SOLVE = 1, TM_ASSEMBLE = 2, TM_LDLT = 3, TM_DSOLVE = 4, TM_RESID = 5, TM_COUNT = 6 };
 __device__ __forceinline__ long long* timers(Ctx& c) { return reinterpret_cast<long long*>(c.sc + SC_COUNT + 4); }
 
 // ------------------------------------------------------------------------------------------
@@ -278,8 +279,8 @@ __device__ __noinline__ void pmul(Ctx& c, const double* x, double* y) {
 
 // res = rhs - K sol for the statically-regularised K (the matrix refinement targets,
 // kkt_system.cpp:296-311): top = (P + epsP I) x + A'z, bottom = A x - (Hs + epsA I) z.
-__device__ __noinline__ double kktResidual(Ctx& c, const DevSettings& st, const double* rhs, const double* sol,
-                              double* res, double& rhsNorm) {
+__device__ __noinline__ double kktResidualImpl(Ctx& c, const DevSettings& st, const double* rhs, const double* sol,
+                                  double* res, double& rhsNorm) {
   const int n = c.n, m = c.m;
   const double* xs = sol;
   const double* zs = sol + n;
@@ -311,6 +312,14 @@ __device__ __noinline__ double kktResidual(Ctx& c, const DevSettings& st, const 
   return sqrt(acc2[0]) / rhsNorm;
 }
 
+__device__ double kktResidual(Ctx& c, const DevSettings& st, const double* rhs, const double* sol, double* res,
+                              double& rhsNorm) {
+  const long long t0 = (st.record_timings && threadIdx.x == 0) ? clock64() : 0;
+  const double r = kktResidualImpl(c, st, rhs, sol, res, rhsNorm);
+  if (st.record_timings && threadIdx.x == 0) timers(c)[TM_RESID] += clock64() - t0;
+  return r;
+}
+
 // ------------------------------------------------------------------------------------------
 // dense LDL' of the tiled root (no pivoting) and its solve
 // ------------------------------------------------------------------------------------------
@@ -331,76 +340,86 @@ struct PivotStats {
 
 template <typename T>
 __device__ __forceinline__ T shflT(T v, int src) { return __shfl_sync(0xffffffffu, v, src); }
+__device__ __forceinline__ df64 shflT(df64 v, int src) {
+  return df64(__shfl_sync(0xffffffffu, v.hi, src), __shfl_sync(0xffffffffu, v.lo, src));
+}
 
 // Factors diagonal tile J in place (one warp). Global row of tile row r is J*32 + r.
+// Right-looking elimination in shared memory: lane r owns row r of the lower triangle (entry
+// (r, k) at k*ld + r, conflict-free across lanes) and reads the pivot column as broadcasts. Only
+// the per-pivot regularisation test runs inside the loop, in the tile's own arithmetic; the pivot
+// statistics (exact zero, wrong sign, smallest |D|) are taken once from the final D.
+// Then the inverse of the unit-lower block is formed column by column (lane c solves L y = e_c)
+// and kept transposed in the upper half: Linv(i, c) at i*ld + c.
 template <typename T>
 __device__ void tileFactorDiag(T* A, int J, int nr, int nx, const DevSettings& st, PivotStats* ps) {
   const int r = threadIdx.x & 31;
   const bool regularized = st.linear_solver == 2;
-  T a[32];
-#pragma unroll
-  for (int col = 0; col < 32; ++col) a[col] = (col <= r) ? A[col * kTileLd + r] : A[r * kTileLd + col];
-  int nreg = 0, zero = 0, wrong = 0;
-  double minAbs = INFINITY;
-#pragma unroll
+  const T epsT = (T)st.dynamic_reg_eps, deltaT = (T)st.dynamic_reg_delta;
+  int nreg = 0;
   for (int j = 0; j < 32; ++j) {
-    T dj = shflT(a[j], j);
-    const int g = J * 32 + j;
-    if (g < nr) {
-      const double sg = (g < nx) ? 1.0 : -1.0;
-      if (regularized) {
-        double dd = (double)dj;
-        if (dd * sg < st.dynamic_reg_eps) {
-          dd += sg * st.dynamic_reg_delta;
-          if (dd * sg < st.dynamic_reg_eps) dd = sg * st.dynamic_reg_delta;
+    T dj = A[j * kTileLd + j];
+    if (regularized) {
+      const int g = J * 32 + j;
+      if (g < nr) {
+        const T sg = (g < nx) ? (T)1 : (T)-1;
+        if (dj * sg < epsT) {
+          dj = dj + sg * deltaT;
+          if (dj * sg < epsT) dj = sg * deltaT;
           ++nreg;
-          dj = (T)dd;
         }
-      } else if (dj == (T)0) {
-        zero = 1;
       }
-      if ((double)dj * sg <= 0.0) wrong = 1;
-      const double ad = fabs((double)dj);
-      minAbs = isfinite(ad) ? fmin(minAbs, ad) : NAN;
     }
     const T inv = (T)1 / dj;
-    const T lj = a[j] * inv;
-#pragma unroll
-    for (int k = j + 1; k < 32; ++k) {
-      const T akj = shflT(a[j], k);
-      a[k] -= lj * akj;
+    const T u = (r > j) ? A[j * kTileLd + r] : (T)0;  // unscaled column-j entry of row r
+    const T lr = u * inv;
+    if (r > j) {
+#pragma unroll 4
+      for (int k = j + 1; k <= r; ++k) A[k * kTileLd + r] -= lr * A[j * kTileLd + k];
     }
-    if (r > j) a[j] = lj;
-    else if (r == j) a[j] = dj;
+    __syncwarp();
+    if (r > j) A[j * kTileLd + r] = lr;
+    else if (r == j) A[j * kTileLd + j] = dj;
+    __syncwarp();
+  }
+  // pivot statistics of the real rows of this tile
+  {
+    const int g = J * 32 + r;
+    const bool real = g < nr;
+    const double d = (double)A[r * kTileLd + r];
+    const double sgn = (g < nx) ? 1.0 : -1.0;
+    const unsigned zeroMask = __ballot_sync(0xffffffffu, real && d == 0.0);
+    const unsigned wrongMask = __ballot_sync(0xffffffffu, real && !(d * sgn > 0.0));
+    double ad = real ? fabs(d) : INFINITY;
+    if (real && !isfinite(ad)) ad = NAN;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+      const double o = __shfl_xor_sync(0xffffffffu, ad, off);
+      ad = (isnan(ad) || isnan(o)) ? NAN : fmin(ad, o);
+    }
+    if (r == 0) {
+      ps->nreg += nreg;
+      if (!regularized && zeroMask) ps->zero = 1;
+      if (wrongMask) ps->wrong = 1;
+      ps->minAbs = (isnan(ad) || isnan(ps->minAbs)) ? NAN : fmin(ps->minAbs, ad);
+    }
+  }
+  // Linv column c = r: y_c = 1, y_i = -(L(i,c) + sum_{k=c+1}^{i-1} L(i,k) y_k) for i > c, with
+  // L(i,k) at k*ld + i and y_k kept at k*ld + c (written before it is read, by this lane)
+  {
+    const int c = r;
+    for (int i = c + 1; i < 32; ++i) {
+      T acc0 = A[c * kTileLd + i], acc1 = (T)0;
+      int k = c + 1;
+      for (; k + 1 < i; k += 2) {
+        acc0 += A[k * kTileLd + i] * A[k * kTileLd + c];
+        acc1 += A[(k + 1) * kTileLd + i] * A[(k + 1) * kTileLd + c];
+      }
+      if (k < i) acc0 += A[k * kTileLd + i] * A[k * kTileLd + c];
+      A[i * kTileLd + c] = -(acc0 + acc1);
+    }
   }
   __syncwarp();
-#pragma unroll
-  for (int col = 0; col < 32; ++col)
-    if (col <= r) A[col * kTileLd + r] = a[col];
-  __syncwarp();
-  // Linv (unit lower): row r by forward substitution, stored transposed in the upper half
-  T iv[32];
-#pragma unroll
-  for (int col = 0; col < 32; ++col) iv[col] = (col == r) ? (T)1 : (T)0;
-#pragma unroll
-  for (int k = 0; k < 32; ++k) {
-    const T lrk = (r > k) ? A[k * kTileLd + r] : (T)0;
-#pragma unroll
-    for (int col = 0; col <= k; ++col) {
-      const T v = (col == k) ? (T)1 : shflT(iv[col], k);
-      iv[col] -= lrk * v;
-    }
-  }
-#pragma unroll
-  for (int col = 0; col < 32; ++col)
-    if (col < r) A[r * kTileLd + col] = iv[col];
-  // every lane saw the same (shuffled) pivots, so lane 0's statistics are the tile's
-  if (r == 0) {
-    ps->nreg += nreg;
-    ps->zero |= zero;
-    ps->wrong |= wrong;
-    ps->minAbs = (isnan(minAbs) || isnan(ps->minAbs)) ? NAN : fmin(ps->minAbs, minAbs);
-  }
 }
 
 // L_IJ = A_IJ Linv_JJ^T D_J^-1 for one off-diagonal tile (one warp), in place. Column c of the
@@ -416,6 +435,7 @@ __device__ void tileOffDiag(T* Aij, const T* Ajj) {
     for (int i = 0; i < 4; ++i)
 #pragma unroll
       for (int j = 0; j < 4; ++j) acc[i][j] = (T)0;
+#pragma unroll 2
     for (int k = 0; k < 32; ++k) {
       T av[4], cv[4];
 #pragma unroll
@@ -454,6 +474,7 @@ __device__ void tileSyrk(T* C, const T* A, const T* B, const T* Ajj) {
     for (int i = 0; i < 4; ++i)
 #pragma unroll
       for (int j = 0; j < 4; ++j) acc[i][j] = (T)0;
+#pragma unroll 2
     for (int k = 0; k < 32; ++k) {
       const T dk = Ajj[k * kTileLd + k];
       T av[4], bv[4];
@@ -573,6 +594,7 @@ __device__ __noinline__ void assembleFactor(Ctx& c, const DevSettings& st, T* M,
   const InstanceDesc& D = *c.D;
   const int n = c.n, nr = c.nr;
   const double epsA = st.static_reg_A + ea;
+  const long long t0 = (st.record_timings && threadIdx.x == 0) ? clock64() : 0;
   // G_u = (Hs_u + epsA I)^-1 as eigenvalues (NN: cu[row]; SOC: sp.r0..r2), then
   // T_u = G_u Ad_u column by column
   FOR_T(u, c.nUnits) {
@@ -610,7 +632,12 @@ __device__ __noinline__ void assembleFactor(Ctx& c, const DevSettings& st, T* M,
     M[c.tgtIdx[t]] += (T)acc;
   }
   __syncthreads();
+  const long long t1 = (st.record_timings && threadIdx.x == 0) ? clock64() : 0;
   denseLdlt<T>(c, M, st, fail, wrongSign, minAbsD);
+  if (st.record_timings && threadIdx.x == 0) {
+    timers(c)[TM_ASSEMBLE] += t1 - t0;
+    timers(c)[TM_LDLT] += clock64() - t1;
+  }
 }
 
 // sol = Kreg^-1 rhs through the factored root (T) with the bump ea used at factorisation.
@@ -636,7 +663,9 @@ __device__ __noinline__ void reducedSolve(Ctx& c, const DevSettings& st, const T
   FOR_T(r, p) y[n + r] = (T)r2[r];
   for (int i = nr + (int)threadIdx.x; i < rootTiles(nr) * kTile; i += blockDim.x) y[i] = (T)0;
   __syncthreads();
+  const long long t0 = (st.record_timings && threadIdx.x == 0) ? clock64() : 0;
   denseSolve<T>(c, M, y);
+  if (st.record_timings && threadIdx.x == 0) timers(c)[TM_DSOLVE] += clock64() - t0;
   FOR_T(j, n) sol[j] = (double)y[j];
   FOR_T(r, p) sol[n + r] = (double)y[n + r];
   __syncthreads();
@@ -666,15 +695,24 @@ __device__ __noinline__ void reducedSolve(Ctx& c, const DevSettings& st, const T
 
 // Factorisation state of the current iteration.
 struct FactState {
-  int use64;      // factor currently held in FP64 (root64)
+  int use64;      // the high-precision factor (in root64) is the one held
   double ep, ea;  // bumps of the held factor
 };
 
 template <typename FT>
 __device__ __forceinline__ FT* rootT(Ctx& c) { return reinterpret_cast<FT*>(c.root); }
 
+// Arithmetic of the high-precision factor held in root64: FP64 for the FP64 kernel, double-float
+// (FP32 pipe, ~48 bits) as the fallback of the mixed-precision kernel.
+template <typename FT> struct HighT { using type = double; };
+template <> struct HighT<float> { using type = df64; };
+template <typename FT>
+__device__ __forceinline__ typename HighT<FT>::type* rootHigh(Ctx& c) {
+  return reinterpret_cast<typename HighT<FT>::type*>(c.root64);
+}
+
 // factorizeWithRetry (kkt_system.cpp:242-264) on the reduced system. In MIXED precision an FP32
-// factor with a wrong-signed pivot is replaced by the FP64 factor (sticky).
+// factor with a wrong-signed pivot is replaced by the double-float factor (sticky).
 template <typename FT>
 __device__ __noinline__ bool factorizeWithRetryImpl(Ctx& c, const DevSettings& st, FactState& fs) {
   double ep = 0.0, ea = 0.0;
@@ -690,7 +728,7 @@ __device__ __noinline__ bool factorizeWithRetryImpl(Ctx& c, const DevSettings& s
         continue;
       }
     } else {
-      assembleFactor<double>(c, st, c.root64, ep, ea, fail, wrong, mind);
+      assembleFactor<typename HighT<FT>::type>(c, st, rootHigh<FT>(c), ep, ea, fail, wrong, mind);
     }
     if (threadIdx.x == 0) c.sc[SC_ATTEMPTS] += 1.0;
     if (!fail && isfinite(mind) && mind > st.dynamic_reg_eps) {
@@ -707,7 +745,7 @@ __device__ __noinline__ bool factorizeWithRetryImpl(Ctx& c, const DevSettings& s
 template <typename FT>
 __device__ void solveOnce(Ctx& c, const DevSettings& st, const FactState& fs, const double* rhs, double* sol) {
   if (fs.use64)
-    reducedSolve<double>(c, st, c.root64, fs.ea, rhs, sol);
+    reducedSolve<typename HighT<FT>::type>(c, st, rootHigh<FT>(c), fs.ea, rhs, sol);
   else
     reducedSolve<FT>(c, st, rootT<FT>(c), fs.ea, rhs, sol);
 }
@@ -719,7 +757,7 @@ __device__ __noinline__ bool vecFinite(Ctx& c, const double* v, int len) {
 }
 
 // KktSystem::solve (kkt_system.cpp:296-311) incl. escalateAndResolve (:266-294), plus the
-// MIXED-precision FP64 fallback. Returns the final relative residual.
+// MIXED-precision fallback to the double-float factor. Returns the final relative residual.
 template <typename FT>
 __device__ bool factorizeWithRetry(Ctx& c, const DevSettings& st, FactState& fs);
 
@@ -738,7 +776,7 @@ __device__ __noinline__ double kktSolveImpl(Ctx& c, const DevSettings& st, FactS
         int fail = 0, wrong = 0;
         double mind = 0.0;
         if (fs.use64)
-          assembleFactor<double>(c, st, c.root64, ep, ea, fail, wrong, mind);
+          assembleFactor<typename HighT<FT>::type>(c, st, rootHigh<FT>(c), ep, ea, fail, wrong, mind);
         else
           assembleFactor<FT>(c, st, rootT<FT>(c), ep, ea, fail, wrong, mind);
         if (fail || !isfinite(mind) || !(mind > st.dynamic_reg_eps)) continue;
@@ -761,13 +799,13 @@ __device__ __noinline__ double kktSolveImpl(Ctx& c, const DevSettings& st, FactS
       rel = kktResidual(c, st, rhs, sol, c.res, rhsNorm);
       ++steps;
       // an FP32 factor whose refinement contracts by less than 4x per step will not reach the
-      // tolerance in the remaining steps: go to the FP64 factor now
+      // tolerance in the remaining steps: go to the high-precision factor now
       if (fp32Factor && !(rel <= st.mixed_fallback_tol) && !(rel <= 0.25 * prev)) break;
     }
     if (threadIdx.x == 0) c.sc[SC_RSTEPS] += steps;
     const bool mixedFp32 = (sizeof(FT) == 4) && !fs.use64;
     if (mixedFp32 && !(rel <= st.mixed_fallback_tol)) {
-      // sticky FP64 fallback: refactor in FP64 (with the retry ladder) and redo this solve
+      // sticky fallback: refactor in double-float (with the retry ladder) and redo this solve
       fs.use64 = 1;
       if (threadIdx.x == 0) c.sc[SC_NFB] += 1.0;
       if (!factorizeWithRetry<FT>(c, st, fs)) return INFINITY;
@@ -814,7 +852,7 @@ __device__ __noinline__ void solveInstance(Ctx& c, const LaunchArgs& a, int inst
   int iterations = 0;
   double dqx = 0, dbz = 0, dsz = 0, dxPx = 0, rtau = 0;
   if (threadIdx.x < SC_COUNT) c.sc[threadIdx.x] = 0.0;
-  if (threadIdx.x < 2) timers(c)[threadIdx.x] = 0;
+  if (threadIdx.x < TM_COUNT) timers(c)[threadIdx.x] = 0;
   const long long tStart = clock64();
   __syncthreads();
 
@@ -1087,9 +1125,12 @@ __device__ __noinline__ void solveInstance(Ctx& c, const LaunchArgs& a, int inst
     double* Bs = a.bwd + D.bwdOff;
     const BwdLayout bl = bwdLayout(c.nr, n, m, c.nsoc);
     const int64_t rs = rootSize(c.nr);
-    if (fs.use64 || sizeof(FT) == 8) {
+    if (sizeof(FT) == 8) {
       const double* R = fs.use64 ? c.root64 : reinterpret_cast<const double*>(c.root);
       for (int64_t t = threadIdx.x; t < rs; t += blockDim.x) Bs[bl.root + t] = R[t];
+    } else if (fs.use64) {
+      const auto* R = rootHigh<FT>(c);
+      for (int64_t t = threadIdx.x; t < rs; t += blockDim.x) Bs[bl.root + t] = (double)R[t];
     } else {
       const FT* R = rootT<FT>(c);
       for (int64_t t = threadIdx.x; t < rs; t += blockDim.x) Bs[bl.root + t] = (double)R[t];
@@ -1145,6 +1186,10 @@ __device__ __noinline__ void solveInstance(Ctx& c, const LaunchArgs& a, int inst
     R.cycles[1] = timers(c)[TM_FACTOR];
     R.cycles[2] = timers(c)[TM_SOLVE];
     R.cycles[3] = tot - R.cycles[1] - R.cycles[2];
+    R.cycles[4] = timers(c)[TM_ASSEMBLE];
+    R.cycles[5] = timers(c)[TM_LDLT];
+    R.cycles[6] = timers(c)[TM_DSOLVE];
+    R.cycles[7] = timers(c)[TM_RESID];
     a.results[inst] = R;
   }
   __syncthreads();
@@ -1183,13 +1228,14 @@ __device__ void setupCtx(Ctx& c, const LaunchArgs& a, int inst, unsigned char* s
   double* q = vb;
   auto take = [&](int len) { double* r = q; q += (len + 1) & ~1; return r; };
   c.x = take(nM); c.rx = take(nM); c.x1 = take(nM); c.Px1 = take(nM); c.dx = take(nM); c.tn = take(nM);
-  c.s = take(mM); c.z = take(mM); c.rz = take(mM); c.z1 = take(mM); c.dz = take(mM); c.ds = take(mM);
+  c.s = take(mM); c.z = take(mM); c.rz = take(mM); c.dz = take(mM); c.ds = take(mM);
   c.dcon = take(mM); c.lam = take(mM); c.tm = take(mM); c.tm2 = take(mM); c.cw = take(mM); c.cu = take(mM);
-  c.ev = take(mM);
   c.rhs = take(NM); c.sol = take(NM); c.res = take(NM); c.cor = take(NM);
   c.rr = take(rM);
   c.sp = reinterpret_cast<SocScale*>(take(8 * L.nsocMax));
-  (void)take(rM);  // spare root-length vector (kept for the layout count)
+  // used once or twice per iteration: always in scratch (vecGlobalDoubles)
+  c.ev = scratch + D.sVecG;
+  c.z1 = c.ev + ((mM + 1) & ~1);
   c.root = L.rootInSmem ? reinterpret_cast<void*>(smem + L.rootOff) : reinterpret_cast<void*>(c.root64);
   c.red = reinterpret_cast<double*>(smem + L.redOff);
   c.sc = c.red + 128;
@@ -1200,7 +1246,7 @@ __device__ void setupCtx(Ctx& c, const LaunchArgs& a, int inst, unsigned char* s
 // kernel: persistent CTAs over an atomic instance queue
 // ------------------------------------------------------------------------------------------
 template <typename FT>
-__global__ void __launch_bounds__(512) ipmKernel(LaunchArgs a) {
+__global__ void __launch_bounds__(256) ipmKernel(LaunchArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ int sInst;
   __shared__ int sRedi[4];
@@ -1280,7 +1326,7 @@ __device__ __noinline__ void adjointInstance(Ctx& c, const LaunchArgs& a) {
   __syncthreads();
 }
 
-__global__ void __launch_bounds__(512) adjointKernel(LaunchArgs a) {
+__global__ void __launch_bounds__(256) adjointKernel(LaunchArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ int sInst;
   __shared__ int sRedi[4];
@@ -1331,6 +1377,84 @@ cudaError_t ipmOccupancy(int* blocksPerSM, int block, size_t smem, bool fp32) {
   e = cudaFuncSetAttribute(ipmKernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocksPerSM, ipmKernel<double>, block, smem);
+}
+
+}  // namespace cxg
+
+// ------------------------------------------------------------------------------------------
+// diagnostic: the dense root LDL' and solve of the IPM kernel on one given matrix (one CTA)
+// ------------------------------------------------------------------------------------------
+namespace cxg {
+
+template <typename T>
+__global__ void __launch_bounds__(256) denseProbeKernel(int nr, int nx, const double* K, const double* b,
+                                                         DevSettings st, double* Lout, double* Dout, double* xout,
+                                                         long long* cyc, int* flags) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ Ctx c;
+  __shared__ double scArea[160];
+  T* M = reinterpret_cast<T*>(smem);
+  const int Tn = rootTiles(nr);
+  const int64_t rs = rootSize(nr);
+  T* y = M + rs;
+  if (threadIdx.x == 0) {
+    c.nr = nr;
+    c.n = nx;
+    c.red = scArea;
+    c.sc = scArea + 128;
+  }
+  for (int64_t t = threadIdx.x; t < rs; t += blockDim.x) M[t] = (T)0;
+  __syncthreads();
+  for (int i = nr + (int)threadIdx.x; i < Tn * kTile; i += blockDim.x) M[rootIdx(nr, i, i)] = (T)1;
+  for (int t = threadIdx.x; t < nr * nr; t += blockDim.x) {
+    const int i = t % nr, j = t / nr;
+    if (i >= j) M[rootIdx(nr, i, j)] = (T)K[t];
+  }
+  __syncthreads();
+  int fail = 0, wrong = 0;
+  double mind = 0.0;
+  const long long t0 = clock64();
+  denseLdlt<T>(c, M, st, fail, wrong, mind);
+  const long long t1 = clock64();
+  for (int t = threadIdx.x; t < nr * nr; t += blockDim.x) {
+    const int i = t % nr, j = t / nr;
+    Lout[t] = (i > j) ? (double)M[rootIdx(nr, i, j)] : ((i == j) ? 1.0 : 0.0);
+  }
+  for (int i = threadIdx.x; i < nr; i += blockDim.x) Dout[i] = (double)M[rootIdx(nr, i, i)];
+  for (int i = threadIdx.x; i < Tn * kTile; i += blockDim.x) y[i] = (i < nr) ? (T)b[i] : (T)0;
+  __syncthreads();
+  const long long t2 = clock64();
+  denseSolve<T>(c, M, y);
+  const long long t3 = clock64();
+  for (int i = threadIdx.x; i < nr; i += blockDim.x) xout[i] = (double)y[i];
+  if (threadIdx.x == 0) {
+    cyc[0] = t1 - t0;
+    cyc[1] = t3 - t2;
+    flags[0] = fail;
+    flags[1] = wrong;
+  }
+}
+
+template <typename T>
+static cudaError_t probeLaunch(int nr, int nx, const double* K, const double* b, const DevSettings& st, int threads,
+                               double* L, double* D, double* x, long long* cyc, int* flags) {
+  const size_t smem = (size_t)(rootSize(nr) + (int64_t)rootTiles(nr) * kTile) * sizeof(T);
+  cudaError_t e = cudaFuncSetAttribute(denseProbeKernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  denseProbeKernel<T><<<1, threads, smem>>>(nr, nx, K, b, st, L, D, x, cyc, flags);
+  return cudaGetLastError();
+}
+
+size_t denseProbeSmem(int arith, int nr) {
+  const size_t elem = (arith == 1) ? 4 : 8;
+  return (size_t)(rootSize(nr) + (int64_t)rootTiles(nr) * kTile) * elem;
+}
+
+cudaError_t launchDenseProbe(int arith, int nr, int nx, const double* K, const double* b, const DevSettings& st,
+                             int threads, double* L, double* D, double* x, long long* cyc, int* flags) {
+  if (arith == 1) return probeLaunch<float>(nr, nx, K, b, st, threads, L, D, x, cyc, flags);
+  if (arith == 2) return probeLaunch<df64>(nr, nx, K, b, st, threads, L, D, x, cyc, flags);
+  return probeLaunch<double>(nr, nx, K, b, st, threads, L, D, x, cyc, flags);
 }
 
 }  // namespace cxg

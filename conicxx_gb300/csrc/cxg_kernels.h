@@ -19,9 +19,12 @@ struct SmemLayout {
 // Doubles of FP64 vectors per CTA for given maxima (must match the carve-up in ipmKernel).
 inline int64_t vecDoubles(int nMax, int mMax, int nrMax, int nsocMax) {
   auto r2 = [](int64_t v) { return (v + 1) & ~int64_t(1); };
-  return 6 * r2(nMax) + 13 * r2(mMax) + 4 * r2((int64_t)nMax + mMax) + 2 * (int64_t)rootTiles(nrMax) * kTile +
+  return 6 * r2(nMax) + 11 * r2(mMax) + 4 * r2((int64_t)nMax + mMax) + (int64_t)rootTiles(nrMax) * kTile +
          r2(8 * (int64_t)nsocMax);
 }
+// Vectors used once or twice per iteration (the cone identity e and the constant-solve z1), kept
+// in the CTA's scratch so the shared-memory vector area stays small enough for the largest root.
+inline int64_t vecGlobalDoubles(int mMax) { return 2 * ((int64_t)(mMax + 1) & ~int64_t(1)); }
 
 struct LaunchArgs {
   const InstanceDesc* desc;
@@ -60,5 +63,13 @@ cudaError_t launchIpm(const LaunchArgs& a, int grid, int block, size_t smem, boo
 cudaError_t launchAdjoint(const LaunchArgs& a, int grid, int block, size_t smem, cudaStream_t stream);
 // Resident CTAs per SM of the IPM kernel for a block size and dynamic shared-memory size.
 cudaError_t ipmOccupancy(int* blocksPerSM, int block, size_t smem, bool fp32);
+
+// Diagnostic: factor the dense symmetric nr x nr matrix K (column-major, first nx pivots
+// expected positive, the rest negative) with the IPM kernel's tiled root LDL' in the given
+// arithmetic (0 FP64, 1 FP32, 2 double-float) on one CTA of `threads` threads, then solve K x = b.
+// Outputs L (unit lower, column-major), D, x, cycles {ldlt, solve}, flags {fail, wrong sign}.
+size_t denseProbeSmem(int arith, int nr);
+cudaError_t launchDenseProbe(int arith, int nr, int nx, const double* K, const double* b, const DevSettings& st,
+                             int threads, double* L, double* D, double* x, long long* cyc, int* flags);
 
 }  // namespace cxg

@@ -84,6 +84,7 @@ struct InstanceDesc {
   int64_t sPv, sAv, sAd, sT, sQ, sB;  // scaled P (user order, then CSR order), scaled A, Ad, T, q, b
   int64_t sRoot64;                    // FP64 root (fallback / FP64 precision when not in SMEM)
   int64_t sVec;                       // FP64 vectors that do not fit in shared memory
+  int64_t sVecG;                      // FP64 vectors always kept in scratch (vecGlobalDoubles)
   int64_t scratchDoubles;             // total per-CTA scratch this instance needs
   int64_t bwdOff;                     // offset of this instance's saved final state (differentiable)
   double cost;                        // scheduling weight (~ nr^3)
@@ -123,7 +124,8 @@ struct DevResult {
   int status, iterations, fp64_fallbacks, refine_steps;
   double objective, primal_residual, dual_residual, duality_gap, mu, max_relres;
   int factor_attempts, error_code;  // error_code: 0 ok, else an internal diagnostic (bounds etc.)
-  long long cycles[4];              // record_timings: total, factorisation, KKT solves, residual/cones
+  long long cycles[8];              // record_timings: total, factorisation, KKT solves, residual/cones,
+                                    // assembly, dense LDL', dense triangular solves, KKT residuals
 };
 
 }  // namespace cxg

@@ -85,12 +85,14 @@ typedef struct cxg_settings {
   int linear_solver;          /* CXG_LINSOLVER_QDLDL */
   /* ---- GB300 additions ---- */
   int precision;              /* CXG_PRECISION_FP64 for cxg_solver, MIXED for cxg_batch */
-  int mixed_refine_max_iter;  /* refinement steps allowed on an FP32 factor before the FP64
-                                 refactorisation fallback (default 4; a step contracting the
-                                 residual by less than 4x falls back at once) */
+  int mixed_refine_max_iter;  /* refinement steps allowed on an FP32 factor before the
+                                 high-precision refactorisation fallback (default 4; a step
+                                 contracting the residual by less than 4x falls back at once) */
   double mixed_fallback_tol;  /* relative KKT residual above which an FP32-factor solve is redone
-                                 with an FP64 factor (default 1e-10) */
-  int threads_per_instance;   /* 0 = autotuned; else 64/128/256/512 */
+                                 with the high-precision factor: double-float arithmetic (about
+                                 48 bits) on the FP32 pipe (default 1e-10) */
+  int threads_per_instance;   /* 0 = by root size (64 up to 64 rows, 128 up to 128, else 256);
+                                 else 64, 128 or 256 */
   int differentiable;         /* keep each instance's final factorisation, scaling and iterate on the
                                  device so backward() can reuse them (default 0; cxg_solver: 1) */
 } cxg_settings;
@@ -106,13 +108,20 @@ typedef struct cxg_info {
   double mu;
   double setup_time_s;
   double solve_time_s;
-  int fp64_fallbacks;         /* KKT solves redone with an FP64 factor (mixed precision) */
+  int fp64_fallbacks;         /* mixed precision: switches to the high-precision (double-float)
+                                 factor after an FP32 factor fell short */
   int refine_steps;           /* total refinement steps taken */
   double max_relres;          /* worst final relative KKT residual over all solves */
   /* with settings.record_timings: device time split of this instance's solve, seconds */
   double time_factor_s;       /* KKT assembly + LDL' factorisations */
   double time_kkt_solve_s;    /* KKT solves incl. iterative refinement */
   double time_other_s;        /* residuals, cone algebra, step lengths */
+  /* with settings.record_timings: parts of the above, seconds */
+  double time_assemble_s;     /* reduced-KKT assembly (inside time_factor_s / fallback refactors) */
+  double time_ldlt_s;         /* dense LDL' of the reduced root */
+  double time_dense_solve_s;  /* triangular solves with the root factor */
+  double time_residual_s;     /* KKT residuals of the refinement */
+  int factor_attempts;        /* factorisations attempted (retry ladder and fallback included) */
 } cxg_info;
 
 /* One problem instance; all pointers are caller-owned host memory (copied, never retained). */
@@ -238,6 +247,16 @@ int cxg_batch_describe(const cxg_batch* batch, char* buf, int buflen);
 int cxg_cones_eval(int op, int zero_dim, int nonneg_dim, int n_soc, const int* soc_dims, const double* s,
                    const double* z, const double* u, const double* v, double alpha_or_eps, double* out,
                    double* scalars, double* soc_params);
+/* Dense root factorisation of the IPM kernel (the reduced KKT root's LDL', QDLDL-style no
+ * pivoting with the per-pivot rule of RegularizedLdlt::regularizePivot when linear_solver is
+ * CXG_LINSOLVER_REGULARIZED, src/conicxx/kkt/regularized_ldlt.cpp:132-139) on one given dense
+ * symmetric matrix K (nr x nr, column-major; pivots < nx expected positive, the rest negative),
+ * run by one CTA of `threads` (32..256, a multiple of 32) threads in arith 0 = FP64, 1 = FP32, 2 = double-float; then the
+ * triangular solves for K x = b. Outputs (each may be NULL): L (nr x nr unit lower, column-major),
+ * D (nr), x (nr), cycles[2] = SM clock cycles of {factorisation, solve}, flags[2] = {exact zero /
+ * too many corrections, wrong-signed pivot}. Allocates its own device buffers. */
+int cxg_dense_ldlt(int nr, int nx, const double* K, const double* b, int arith, int threads, int linear_solver,
+                   double* L, double* D, double* x, long long* cycles, int* flags);
 /* Host equilibration of the set-up path (Equilibration::compute, src/conicxx/kkt/equilibration.cpp:8-100):
  * d (n), e (m), c. No GPU needed. */
 int cxg_equilibration(const cxg_problem* problem, const cxg_settings* settings, double* d, double* e, double* c);
