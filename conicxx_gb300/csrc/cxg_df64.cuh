@@ -75,6 +75,21 @@ __device__ __forceinline__ df64 operator/(df64 a, df64 b) {
   return df64(h, l);
 }
 
+// c + a * b with one renormalisation: the exact product of the high parts (TwoProduct), the
+// cross terms folded into its error, then one TwoSum with c.hi (15 float operations instead of
+// the 18 of a separate multiply and add).
+__device__ __forceinline__ df64 dfMad(df64 c, df64 a, df64 b) {
+  const float ph = __fmul_rn(a.hi, b.hi);
+  float pl = __fmaf_rn(a.hi, b.hi, -ph);
+  pl = __fmaf_rn(a.hi, b.lo, pl);
+  pl = __fmaf_rn(a.lo, b.hi, pl);
+  float s, e, h, l;
+  dfTwoSum(c.hi, ph, s, e);
+  e = __fadd_rn(e, __fadd_rn(c.lo, pl));
+  dfFastTwoSum(s, e, h, l);
+  return df64(h, l);
+}
+
 __device__ __forceinline__ df64& operator+=(df64& a, df64 b) { return a = a + b; }
 __device__ __forceinline__ df64& operator-=(df64& a, df64 b) { return a = a - b; }
 __device__ __forceinline__ df64& operator*=(df64& a, df64 b) { return a = a * b; }

@@ -343,22 +343,79 @@ __device__ __forceinline__ T shflT(T v, int src) { return __shfl_sync(0xffffffff
 __device__ __forceinline__ df64 shflT(df64 v, int src) {
   return df64(__shfl_sync(0xffffffffu, v.hi, src), __shfl_sync(0xffffffffu, v.lo, src));
 }
+// c + a b and c - a b in the tile arithmetic (one FMA for float/double, the fused double-float form)
+template <typename T>
+__device__ __forceinline__ T madT(T c, T a, T b) { return c + a * b; }
+__device__ __forceinline__ df64 madT(df64 c, df64 a, df64 b) { return dfMad(c, a, b); }
+template <typename T>
+__device__ __forceinline__ T msubT(T c, T a, T b) { return c - a * b; }
+__device__ __forceinline__ df64 msubT(df64 c, df64 a, df64 b) { return dfMad(c, -a, b); }
+
+// A row of 32 values held in registers (indices are compile-time after unrolling). The
+// double-float row is kept as two float arrays so that it stays in registers.
+template <typename T>
+struct Row32 {
+  T v[32];
+  __device__ __forceinline__ T get(int k) const { return v[k]; }
+  __device__ __forceinline__ void set(int k, T x) { v[k] = x; }
+};
+template <>
+struct Row32<df64> {
+  float h[32], l[32];
+  __device__ __forceinline__ df64 get(int k) const { return df64(h[k], l[k]); }
+  __device__ __forceinline__ void set(int k, df64 x) {
+    h[k] = x.hi;
+    l[k] = x.lo;
+  }
+};
+
+// 1/d for a pivot. FP32: the IEEE reciprocal intrinsic. FP64 and double-float: Newton-Raphson
+// iteration r <- r + r (1 - d r) from the FP32 reciprocal of the leading part (each step doubles
+// the correct bits: 23 -> 46 -> full), falling back to a division when d is outside the float
+// range or not finite.
+__device__ __forceinline__ float recipT(float d) { return __frcp_rn(d); }
+__device__ __forceinline__ double recipT(double d) {
+  const float f = __double2float_rn(d);
+  const float af = fabsf(f);
+  if (!(af >= 1e-37f && af <= 1e37f)) return 1.0 / d;
+  double r = (double)__frcp_rn(f);
+  double e = fma(-d, r, 1.0);
+  r = fma(r, e, r);
+  e = fma(-d, r, 1.0);
+  return fma(r, e, r);
+}
+__device__ __forceinline__ df64 recipT(df64 d) {
+  const float af = fabsf(d.hi);
+  if (!(af >= 1e-37f && af <= 1e37f)) return df64(1.0f, 0.0f) / d;
+  df64 r(__frcp_rn(d.hi), 0.0f);
+  const df64 one(1.0f, 0.0f);
+  r = r + r * (one - d * r);
+  return r + r * (one - d * r);
+}
 
 // Factors diagonal tile J in place (one warp). Global row of tile row r is J*32 + r.
-// Right-looking elimination in shared memory: lane r owns row r of the lower triangle (entry
-// (r, k) at k*ld + r, conflict-free across lanes) and reads the pivot column as broadcasts. Only
-// the per-pivot regularisation test runs inside the loop, in the tile's own arithmetic; the pivot
+// Lane r keeps row r of the tile in registers (entries right of the diagonal mirrored from the
+// lower triangle) and the 32 elimination steps broadcast pivot column j by shuffles. The same
+// steps applied to the identity (Gauss-Jordan) give row r of the inverse of the unit-lower
+// factor, which is stored transposed in the upper half: Linv(r, c) at r*ld + c. Only the
+// per-pivot regularisation test runs inside the loop, in the tile's own arithmetic; the pivot
 // statistics (exact zero, wrong sign, smallest |D|) are taken once from the final D.
-// Then the inverse of the unit-lower block is formed column by column (lane c solves L y = e_c)
-// and kept transposed in the upper half: Linv(i, c) at i*ld + c.
 template <typename T>
 __device__ void tileFactorDiag(T* A, int J, int nr, int nx, const DevSettings& st, PivotStats* ps) {
   const int r = threadIdx.x & 31;
   const bool regularized = st.linear_solver == 2;
   const T epsT = (T)st.dynamic_reg_eps, deltaT = (T)st.dynamic_reg_delta;
+  Row32<T> a, e;
+#pragma unroll
+  for (int col = 0; col < 32; ++col) {
+    a.set(col, (col <= r) ? A[col * kTileLd + r] : A[r * kTileLd + col]);
+    e.set(col, (col == r) ? (T)1 : (T)0);
+  }
   int nreg = 0;
+  T dr = (T)0;
+#pragma unroll
   for (int j = 0; j < 32; ++j) {
-    T dj = A[j * kTileLd + j];
+    T dj = shflT(a.get(j), j);
     if (regularized) {
       const int g = J * 32 + j;
       if (g < nr) {
@@ -370,23 +427,30 @@ __device__ void tileFactorDiag(T* A, int J, int nr, int nx, const DevSettings& s
         }
       }
     }
-    const T inv = (T)1 / dj;
-    const T u = (r > j) ? A[j * kTileLd + r] : (T)0;  // unscaled column-j entry of row r
-    const T lr = u * inv;
-    if (r > j) {
-#pragma unroll 4
-      for (int k = j + 1; k <= r; ++k) A[k * kTileLd + r] -= lr * A[j * kTileLd + k];
+    const T inv = recipT(dj);
+    const T lj = a.get(j) * inv;
+#pragma unroll
+    for (int k = j + 1; k < 32; ++k) {
+      const T akj = shflT(a.get(j), k);
+      a.set(k, msubT(a.get(k), lj, akj));
     }
-    __syncwarp();
-    if (r > j) A[j * kTileLd + r] = lr;
-    else if (r == j) A[j * kTileLd + j] = dj;
-    __syncwarp();
+    // Gauss-Jordan on the identity: row j of the inverse is final at step j
+#pragma unroll
+    for (int c = 0; c <= j; ++c) {
+      const T ejc = shflT(e.get(c), j);
+      if (r > j) e.set(c, msubT(e.get(c), lj, ejc));
+    }
+    if (r > j) a.set(j, lj);
+    if (r == j) {
+      a.set(j, dj);
+      dr = dj;
+    }
   }
   // pivot statistics of the real rows of this tile
   {
     const int g = J * 32 + r;
     const bool real = g < nr;
-    const double d = (double)A[r * kTileLd + r];
+    const double d = (double)dr;
     const double sgn = (g < nx) ? 1.0 : -1.0;
     const unsigned zeroMask = __ballot_sync(0xffffffffu, real && d == 0.0);
     const unsigned wrongMask = __ballot_sync(0xffffffffu, real && !(d * sgn > 0.0));
@@ -404,20 +468,11 @@ __device__ void tileFactorDiag(T* A, int J, int nr, int nx, const DevSettings& s
       ps->minAbs = (isnan(ad) || isnan(ps->minAbs)) ? NAN : fmin(ps->minAbs, ad);
     }
   }
-  // Linv column c = r: y_c = 1, y_i = -(L(i,c) + sum_{k=c+1}^{i-1} L(i,k) y_k) for i > c, with
-  // L(i,k) at k*ld + i and y_k kept at k*ld + c (written before it is read, by this lane)
-  {
-    const int c = r;
-    for (int i = c + 1; i < 32; ++i) {
-      T acc0 = A[c * kTileLd + i], acc1 = (T)0;
-      int k = c + 1;
-      for (; k + 1 < i; k += 2) {
-        acc0 += A[k * kTileLd + i] * A[k * kTileLd + c];
-        acc1 += A[(k + 1) * kTileLd + i] * A[(k + 1) * kTileLd + c];
-      }
-      if (k < i) acc0 += A[k * kTileLd + i] * A[k * kTileLd + c];
-      A[i * kTileLd + c] = -(acc0 + acc1);
-    }
+  __syncwarp();
+#pragma unroll
+  for (int col = 0; col < 32; ++col) {
+    if (col <= r) A[col * kTileLd + r] = a.get(col);
+    if (col < r) A[r * kTileLd + col] = e.get(col);
   }
   __syncwarp();
 }
@@ -448,7 +503,7 @@ __device__ void tileOffDiag(T* Aij, const T* Ajj) {
 #pragma unroll
       for (int i = 0; i < 4; ++i)
 #pragma unroll
-        for (int j = 0; j < 4; ++j) acc[i][j] += av[i] * cv[j];
+        for (int j = 0; j < 4; ++j) acc[i][j] = madT(acc[i][j], av[i], cv[j]);
     }
     __syncwarp();
 #pragma unroll
@@ -485,7 +540,7 @@ __device__ void tileSyrk(T* C, const T* A, const T* B, const T* Ajj) {
 #pragma unroll
       for (int i = 0; i < 4; ++i)
 #pragma unroll
-        for (int j = 0; j < 4; ++j) acc[i][j] += av[i] * bv[j];
+        for (int j = 0; j < 4; ++j) acc[i][j] = madT(acc[i][j], av[i], bv[j]);
     }
 #pragma unroll
     for (int j = 0; j < 4; ++j)
@@ -495,7 +550,7 @@ __device__ void tileSyrk(T* C, const T* A, const T* B, const T* Ajj) {
 }
 
 template <typename T>
-__device__ void denseLdlt(Ctx& c, T* M, const DevSettings& st, int& fail, int& wrongSign, double& minAbsD) {
+__device__ __noinline__ void denseLdlt(Ctx& c, T* M, const DevSettings& st, int& fail, int& wrongSign, double& minAbsD) {
   const int nr = c.nr, nx = c.n, Tn = rootTiles(nr);
   const int warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
   PivotStats* ps = reinterpret_cast<PivotStats*>(c.sc + SC_COUNT);
@@ -541,7 +596,7 @@ __device__ void denseSolve(Ctx& c, const T* M, T* y) {
     const T* Ajj = M + tileBase(Tn, J, J);
     if (warp == 0) {
       T acc = y[J * 32 + lane];
-      for (int col = 0; col < lane; ++col) acc += Ajj[lane * kTileLd + col] * y[J * 32 + col];
+      for (int col = 0; col < lane; ++col) acc = madT(acc, Ajj[lane * kTileLd + col], y[J * 32 + col]);
       __syncwarp();
       y[J * 32 + lane] = acc;
     }
@@ -551,7 +606,7 @@ __device__ void denseSolve(Ctx& c, const T* M, T* y) {
       const int I = J + 1 + t / 32, rr = t % 32;
       const T* Lij = M + tileBase(Tn, I, J);
       T acc = (T)0;
-      for (int col = 0; col < 32; ++col) acc += Lij[col * kTileLd + rr] * y[J * 32 + col];
+      for (int col = 0; col < 32; ++col) acc = madT(acc, Lij[col * kTileLd + rr], y[J * 32 + col]);
       y[I * 32 + rr] -= acc;
     }
     __syncthreads();
@@ -566,7 +621,7 @@ __device__ void denseSolve(Ctx& c, const T* M, T* y) {
     const T* Ajj = M + tileBase(Tn, J, J);
     if (warp == 0) {
       T acc = y[J * 32 + lane];
-      for (int row = lane + 1; row < 32; ++row) acc += Ajj[row * kTileLd + lane] * y[J * 32 + row];
+      for (int row = lane + 1; row < 32; ++row) acc = madT(acc, Ajj[row * kTileLd + lane], y[J * 32 + row]);
       __syncwarp();
       y[J * 32 + lane] = acc;
     }
@@ -576,7 +631,7 @@ __device__ void denseSolve(Ctx& c, const T* M, T* y) {
       const int K = t / 32, cc = t % 32;
       const T* Ljk = M + tileBase(Tn, J, K);
       T acc = (T)0;
-      for (int row = 0; row < 32; ++row) acc += Ljk[cc * kTileLd + row] * y[J * 32 + row];
+      for (int row = 0; row < 32; ++row) acc = madT(acc, Ljk[cc * kTileLd + row], y[J * 32 + row]);
       y[K * 32 + cc] -= acc;
     }
     __syncthreads();
