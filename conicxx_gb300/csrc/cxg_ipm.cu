@@ -393,7 +393,7 @@ __device__ __forceinline__ df64 recipT(df64 d) {
   return r + r * (one - d * r);
 }
 
-// Factors diagonal tile J in place (one warp). Global row of tile row r is J*32 + r.
+// Factors diagonal tile J in place (one warp), FP32 form. Global row of tile row r is J*32 + r.
 // Lane r keeps row r of the tile in registers (entries right of the diagonal mirrored from the
 // lower triangle) and the 32 elimination steps broadcast pivot column j by shuffles. The same
 // steps applied to the identity (Gauss-Jordan) give row r of the inverse of the unit-lower
@@ -401,7 +401,7 @@ __device__ __forceinline__ df64 recipT(df64 d) {
 // per-pivot regularisation test runs inside the loop, in the tile's own arithmetic; the pivot
 // statistics (exact zero, wrong sign, smallest |D|) are taken once from the final D.
 template <typename T>
-__device__ void tileFactorDiag(T* A, int J, int nr, int nx, const DevSettings& st, PivotStats* ps) {
+__device__ void tileFactorDiagRegs(T* A, int J, int nr, int nx, const DevSettings& st, PivotStats* ps) {
   const int r = threadIdx.x & 31;
   const bool regularized = st.linear_solver == 2;
   const T epsT = (T)st.dynamic_reg_eps, deltaT = (T)st.dynamic_reg_delta;
@@ -475,6 +475,188 @@ __device__ void tileFactorDiag(T* A, int J, int nr, int nx, const DevSettings& s
     if (col < r) A[r * kTileLd + col] = e.get(col);
   }
   __syncwarp();
+}
+
+// Factors diagonal tile J in place (one warp), form for 8-byte arithmetic (FP64, double-float),
+// whose fully unrolled register version would be too large. Global row of tile row r is J*32 + r.
+// Blocked right-looking LDL' in 8-column blocks, in shared memory (entry (i, k) at k*ld + i):
+//  (1) leaf: the 8x8 diagonal block, rows in registers of its 8 lanes, pivots by shuffle;
+//  (2) panel: every row below finishes its 8 entries of the block by substitution with the leaf
+//      (unscaled values kept in registers for (3)) and scales them by the pivot reciprocals;
+//  (3) trailing: rows below subtract the block's rank-8 product from their remaining entries.
+// Only the per-pivot regularisation test runs inside the pivot loop, in the tile's own
+// arithmetic; the pivot statistics (exact zero, wrong sign, smallest |D|) are taken once from D.
+// Then the inverse of the unit-lower factor, blocked the same way (four 8x8 leaf inverses, then
+// the blocks below the diagonal by distance), is stored transposed in the upper half:
+// Linv(R, C) at R*ld + C for C < R.
+template <typename T>
+__device__ void tileFactorDiagBlocked(T* A, int J, int nr, int nx, const DevSettings& st, PivotStats* ps) {
+  const int r = threadIdx.x & 31;
+  const bool regularized = st.linear_solver == 2;
+  const T epsT = (T)st.dynamic_reg_eps, deltaT = (T)st.dynamic_reg_delta;
+  int nreg = 0;
+  T invMine = (T)0;  // 1 / D(r), kept by lane r
+  for (int b = 0; b < 4; ++b) {
+    const int c0 = 8 * b;
+    const int li = r - c0;
+    const bool leaf = li >= 0 && li < 8;
+    // (1) leaf
+    T a[8];
+#pragma unroll
+    for (int t = 0; t < 8; ++t) {
+      const int ct = c0 + t;
+      a[t] = leaf ? ((t <= li) ? A[ct * kTileLd + r] : A[r * kTileLd + ct]) : (T)0;
+    }
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      T dj = shflT(a[j], c0 + j);
+      if (regularized) {
+        const int g = J * 32 + c0 + j;
+        if (g < nr) {
+          const T sg = (g < nx) ? (T)1 : (T)-1;
+          if (dj * sg < epsT) {
+            dj = dj + sg * deltaT;
+            if (dj * sg < epsT) dj = sg * deltaT;
+            ++nreg;
+          }
+        }
+      }
+      const T inv = recipT(dj);
+      if (li == j) invMine = inv;
+      const T lj = a[j] * inv;
+#pragma unroll
+      for (int k = j + 1; k < 8; ++k) {
+        const T akj = shflT(a[j], c0 + k);
+        a[k] = msubT(a[k], lj, akj);
+      }
+      if (li > j) a[j] = lj;
+      if (li == j) a[j] = dj;
+    }
+    if (leaf) {
+#pragma unroll
+      for (int t = 0; t < 8; ++t)
+        if (t <= li) A[(c0 + t) * kTileLd + r] = a[t];
+    }
+    __syncwarp();
+    if (c0 + 8 >= 32) break;
+    // (2) panel
+    const bool below = r >= c0 + 8;
+    T u[8];
+#pragma unroll
+    for (int t = 0; t < 8; ++t) u[t] = below ? A[(c0 + t) * kTileLd + r] : (T)0;
+#pragma unroll
+    for (int t = 0; t < 8; ++t) {
+#pragma unroll
+      for (int s2 = t + 1; s2 < 8; ++s2) u[s2] = msubT(u[s2], u[t], A[(c0 + t) * kTileLd + c0 + s2]);
+    }
+#pragma unroll
+    for (int t = 0; t < 8; ++t) {
+      const T idt = shflT(invMine, c0 + t);
+      if (below) A[(c0 + t) * kTileLd + r] = u[t] * idt;
+    }
+    __syncwarp();
+    // (3) trailing
+    if (below) {
+      int k = c0 + 8;
+      for (; k + 3 <= r; k += 4) {
+        T acc0 = A[k * kTileLd + r], acc1 = A[(k + 1) * kTileLd + r];
+        T acc2 = A[(k + 2) * kTileLd + r], acc3 = A[(k + 3) * kTileLd + r];
+#pragma unroll
+        for (int t = 0; t < 8; ++t) {
+          const T* Lc = A + (c0 + t) * kTileLd;
+          acc0 = msubT(acc0, u[t], Lc[k]);
+          acc1 = msubT(acc1, u[t], Lc[k + 1]);
+          acc2 = msubT(acc2, u[t], Lc[k + 2]);
+          acc3 = msubT(acc3, u[t], Lc[k + 3]);
+        }
+        A[k * kTileLd + r] = acc0;
+        A[(k + 1) * kTileLd + r] = acc1;
+        A[(k + 2) * kTileLd + r] = acc2;
+        A[(k + 3) * kTileLd + r] = acc3;
+      }
+      for (; k <= r; ++k) {
+        T acc = A[k * kTileLd + r];
+#pragma unroll
+        for (int t = 0; t < 8; ++t) acc = msubT(acc, u[t], A[(c0 + t) * kTileLd + k]);
+        A[k * kTileLd + r] = acc;
+      }
+    }
+    __syncwarp();
+  }
+  // pivot statistics of the real rows of this tile
+  {
+    const int g = J * 32 + r;
+    const bool real = g < nr;
+    const double d = (double)A[r * kTileLd + r];
+    const double sgn = (g < nx) ? 1.0 : -1.0;
+    const unsigned zeroMask = __ballot_sync(0xffffffffu, real && d == 0.0);
+    const unsigned wrongMask = __ballot_sync(0xffffffffu, real && !(d * sgn > 0.0));
+    double ad = real ? fabs(d) : INFINITY;
+    if (real && !isfinite(ad)) ad = NAN;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+      const double o = __shfl_xor_sync(0xffffffffu, ad, off);
+      ad = (isnan(ad) || isnan(o)) ? NAN : fmin(ad, o);
+    }
+    if (r == 0) {
+      ps->nreg += nreg;
+      if (!regularized && zeroMask) ps->zero = 1;
+      if (wrongMask) ps->wrong = 1;
+      ps->minAbs = (isnan(ad) || isnan(ps->minAbs)) ? NAN : fmin(ps->minAbs, ad);
+    }
+  }
+  // (a) inverses of the four 8x8 unit-lower leaf blocks, lane r -> block r/8, column r%8
+  {
+    const int o = r & ~7, c = r & 7;
+    T y[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      T acc = (T)0;
+#pragma unroll
+      for (int k = 0; k < i; ++k) acc = madT(acc, A[(o + k) * kTileLd + o + i], y[k]);
+      y[i] = (i < c) ? (T)0 : ((i == c) ? (T)1 : -acc);
+    }
+#pragma unroll
+    for (int i = 0; i < 8; ++i)
+      if (i > c) A[(o + i) * kTileLd + o + c] = y[i];
+  }
+  __syncwarp();
+  // (b) blocks (I, J) = (Jb + d, Jb): Linv(I,J) = -Linv(I,I) sum_{K=J}^{I-1} L(I,K) Linv(K,J)
+  for (int d = 1; d < 4; ++d) {
+    const int nb = 4 - d;
+    for (int e = r; e < nb * 64; e += 32) {
+      const int Jb = e >> 6, i = (e >> 3) & 7, j = e & 7;
+      const int R = 8 * (Jb + d) + i, C = 8 * Jb + j;
+      T acc0 = (T)0, acc1 = (T)0;
+      for (int kk = 8 * Jb; kk < 8 * (Jb + d); kk += 2) {
+        const T lv0 = (kk > C) ? A[kk * kTileLd + C] : ((kk == C) ? (T)1 : (T)0);
+        const T lv1 = (kk + 1 > C) ? A[(kk + 1) * kTileLd + C] : ((kk + 1 == C) ? (T)1 : (T)0);
+        acc0 = madT(acc0, A[kk * kTileLd + R], lv0);
+        acc1 = madT(acc1, A[(kk + 1) * kTileLd + R], lv1);
+      }
+      A[R * kTileLd + C] = acc0 + acc1;
+    }
+    __syncwarp();
+    if (r < nb * 8) {
+      const int Jb = r >> 3, j = r & 7;
+      const int o = 8 * (Jb + d), C = 8 * Jb + j;
+      for (int i = 7; i >= 0; --i) {
+        T acc = A[(o + i) * kTileLd + C];
+        for (int i2 = 0; i2 < i; ++i2) acc = madT(acc, A[(o + i) * kTileLd + o + i2], A[(o + i2) * kTileLd + C]);
+        A[(o + i) * kTileLd + C] = -acc;
+      }
+    }
+    __syncwarp();
+  }
+}
+
+// Diagonal tile factorisation: the register form for FP32, the blocked form for 8-byte types.
+template <typename T>
+__device__ __forceinline__ void tileFactorDiag(T* A, int J, int nr, int nx, const DevSettings& st, PivotStats* ps) {
+  if constexpr (sizeof(T) == 4)
+    tileFactorDiagRegs<T>(A, J, nr, nx, st, ps);
+  else
+    tileFactorDiagBlocked<T>(A, J, nr, nx, st, ps);
 }
 
 // L_IJ = A_IJ Linv_JJ^T D_J^-1 for one off-diagonal tile (one warp), in place. Column c of the
