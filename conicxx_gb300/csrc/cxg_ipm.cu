@@ -22,6 +22,22 @@ namespace cxg {
 
 #define FOR_T(i, n) for (int i = (int)threadIdx.x; i < (n); i += (int)blockDim.x)
 
+// sum_{k=beg}^{end-1} val[k] * x[col[k]] with four independent accumulators: one accumulator
+// would make every row a dependent FP64 chain, the cost on GB300's narrow FP64 pipe.
+__device__ __forceinline__ double csrDot(const double* __restrict__ val, const int* __restrict__ col, int beg, int end,
+                                         const double* x) {
+  double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+  int k = beg;
+  for (; k + 3 < end; k += 4) {
+    a0 = fma(val[k], x[col[k]], a0);
+    a1 = fma(val[k + 1], x[col[k + 1]], a1);
+    a2 = fma(val[k + 2], x[col[k + 2]], a2);
+    a3 = fma(val[k + 3], x[col[k + 3]], a3);
+  }
+  for (; k < end; ++k) a0 = fma(val[k], x[col[k]], a0);
+  return (a0 + a1) + (a2 + a3);
+}
+
 // Finiteness by the exponent bits (an integer test; FP64 compares run on the scarce FP64 pipe).
 __device__ __forceinline__ bool finiteBits(double v) {
   return ((__double_as_longlong(v) >> 52) & 0x7ff) != 0x7ff;
@@ -269,11 +285,7 @@ __device__ void ensureStrictlyInteriorWarm(Ctx& c, double* v) {
 // ------------------------------------------------------------------------------------------
 // y = P_sym x (full symmetric CSR, one thread per row)
 __device__ __noinline__ void pmul(Ctx& c, const double* x, double* y) {
-  FOR_T(i, c.n) {
-    double acc = 0.0;
-    for (int k = c.psRow[i]; k < c.psRow[i + 1]; ++k) acc += c.Pv[k] * x[c.psCol[k]];
-    y[i] = acc;
-  }
+  FOR_T(i, c.n) y[i] = csrDot(c.Pv, c.psCol, c.psRow[i], c.psRow[i + 1], x);
   __syncthreads();
 }
 
@@ -287,9 +299,8 @@ __device__ __noinline__ double kktResidualImpl(Ctx& c, const DevSettings& st, co
   double acc2[2] = {0.0, 0.0};
   FOR_T(t, n + m) {
     if (t < n) {
-      double acc = st.static_reg_P * xs[t];
-      for (int k = c.psRow[t]; k < c.psRow[t + 1]; ++k) acc += c.Pv[k] * xs[c.psCol[k]];
-      for (int k = c.ap[t]; k < c.ap[t + 1]; ++k) acc += c.Av[k] * zs[c.ai[k]];
+      double acc = st.static_reg_P * xs[t] + csrDot(c.Pv, c.psCol, c.psRow[t], c.psRow[t + 1], xs);
+      acc += csrDot(c.Av, c.ai, c.ap[t], c.ap[t + 1], zs);
       res[t] = rhs[t] - acc;
     } else {
       const int r = t - n;
@@ -743,20 +754,38 @@ __device__ __noinline__ void denseLdlt(Ctx& c, T* M, const DevSettings& st, int&
     ps->minAbs = INFINITY;
   }
   __syncthreads();
-  for (int J = 0; J < Tn; ++J) {
+  // Right-looking by tile column with a one-column lookahead: warp 0 applies column J's update
+  // to the next diagonal tile and factors it while the other warps apply the rest of column J.
+  if (warp == 0) tileFactorDiag<T>(M, 0, nr, nx, st, ps);
+  __syncthreads();
+  for (int J = 0; J + 1 < Tn; ++J) {
     T* Ajj = M + tileBase(Tn, J, J);
-    if (warp == 0) tileFactorDiag<T>(Ajj, J, nr, nx, st, ps);
-    __syncthreads();
     for (int I = J + 1 + warp; I < Tn; I += nw) tileOffDiag<T>(M + tileBase(Tn, I, J), Ajj);
     __syncthreads();
     const int rem = Tn - J - 1;
     const int npairs = rem * (rem + 1) / 2;
-    for (int t = warp; t < npairs; t += nw) {
-      // pair t -> (I, K) with J < K <= I < Tn, enumerated column by column
-      int K = J + 1, tt = t, len = rem;
-      while (tt >= len) { tt -= len; --len; ++K; }
-      const int I = K + tt;
-      tileSyrk<T>(M + tileBase(Tn, I, K), M + tileBase(Tn, I, J), M + tileBase(Tn, K, J), Ajj);
+    if (warp == 0 || nw == 1) {
+      T* Anext = M + tileBase(Tn, J + 1, J + 1);
+      const T* Lnext = M + tileBase(Tn, J + 1, J);
+      tileSyrk<T>(Anext, Lnext, Lnext, Ajj);
+      if (nw == 1) {
+        for (int t = 1; t < npairs; ++t) {
+          int K = J + 1, tt = t, len = rem;
+          while (tt >= len) { tt -= len; --len; ++K; }
+          const int I = K + tt;
+          tileSyrk<T>(M + tileBase(Tn, I, K), M + tileBase(Tn, I, J), M + tileBase(Tn, K, J), Ajj);
+        }
+      }
+      tileFactorDiag<T>(Anext, J + 1, nr, nx, st, ps);
+    } else {
+      // pairs t >= 1: (I, K) with J < K <= I < Tn, enumerated column by column (t = 0 is the
+      // next diagonal tile)
+      for (int t = warp; t < npairs; t += nw - 1) {
+        int K = J + 1, tt = t, len = rem;
+        while (tt >= len) { tt -= len; --len; ++K; }
+        const int I = K + tt;
+        tileSyrk<T>(M + tileBase(Tn, I, K), M + tileBase(Tn, I, J), M + tileBase(Tn, K, J), Ajj);
+      }
     }
     __syncthreads();
   }
@@ -767,29 +796,67 @@ __device__ __noinline__ void denseLdlt(Ctx& c, T* M, const DevSettings& st, int&
   __syncthreads();
 }
 
+template <typename T>
+__device__ __forceinline__ T shflXorT(T v, int m) { return __shfl_xor_sync(0xffffffffu, v, m); }
+__device__ __forceinline__ df64 shflXorT(df64 v, int m) {
+  return df64(__shfl_xor_sync(0xffffffffu, v.hi, m), __shfl_xor_sync(0xffffffffu, v.lo, m));
+}
+
+// Largest split s in {1, 2, 4, 8} of a 32-term dot product such that rows * s threads fit in
+// one pass of the block (rows is a multiple of 32, so each warp holds whole groups of s lanes).
+__device__ __forceinline__ int dotSplit(int rows) {
+  int s = 1;
+  while (s < 8 && rows * s * 2 <= (int)blockDim.x) s *= 2;
+  return s;
+}
+
+// Sum of a dot-product partial over the s consecutive lanes of a group (s a power of two <= 8).
+template <typename T>
+__device__ __forceinline__ T groupSum(T v, int s) {
+  for (int m = 1; m < s; m <<= 1) v = v + shflXorT(v, m);
+  return v;
+}
+
 // y <- M^-1 y for the factored tiled root; y has Tn*32 entries (padding entries are zero).
+// Every block product (the diagonal tile's Linv and each off-diagonal tile) is a set of 32-term
+// dot products, split over s lanes per row (dotSplit) and reduced by shuffles, so that the few
+// rows of the late steps still occupy the whole block.
 template <typename T>
 __device__ void denseSolve(Ctx& c, const T* M, T* y) {
   const int Tn = rootTiles(c.nr);
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int nth = blockDim.x;
   // forward: y_J = Linv_JJ y_J, then y_I -= L_IJ y_J for I > J
   for (int J = 0; J < Tn; ++J) {
     const T* Ajj = M + tileBase(Tn, J, J);
-    if (warp == 0) {
-      T acc = y[J * 32 + lane];
-      for (int col = 0; col < lane; ++col) acc = madT(acc, Ajj[lane * kTileLd + col], y[J * 32 + col]);
-      __syncwarp();
-      y[J * 32 + lane] = acc;
+    T* yJ = y + J * 32;
+    {
+      const int sd = dotSplit(32), w = 32 / sd;
+      T tot = (T)0;
+      int i = 0, p = 0;
+      if ((int)threadIdx.x < 32 * sd) {
+        i = threadIdx.x / sd;
+        p = threadIdx.x % sd;
+        T acc = (T)0;
+        for (int col = p * w; col < (p + 1) * w && col < i; ++col) acc = madT(acc, Ajj[i * kTileLd + col], yJ[col]);
+        tot = groupSum(acc, sd);
+      }
+      __syncthreads();
+      if ((int)threadIdx.x < 32 * sd && p == 0) yJ[i] = yJ[i] + tot;
+      __syncthreads();
     }
-    __syncthreads();
     const int rows = (Tn - J - 1) * 32;
-    for (int t = threadIdx.x; t < rows; t += nth) {
-      const int I = J + 1 + t / 32, rr = t % 32;
-      const T* Lij = M + tileBase(Tn, I, J);
-      T acc = (T)0;
-      for (int col = 0; col < 32; ++col) acc = madT(acc, Lij[col * kTileLd + rr], y[J * 32 + col]);
-      y[I * 32 + rr] -= acc;
+    if (rows > 0) {
+      const int s = dotSplit(rows), w = 32 / s;
+      for (int t = threadIdx.x; t < rows * s; t += nth) {
+        const int row = t / s, p = t % s;
+        const int I = J + 1 + row / 32, rr = row % 32;
+        const T* Lij = M + tileBase(Tn, I, J);
+        T acc = (T)0;
+#pragma unroll 4
+        for (int col = p * w; col < (p + 1) * w; ++col) acc = madT(acc, Lij[col * kTileLd + rr], yJ[col]);
+        acc = groupSum(acc, s);
+        if (p == 0) y[I * 32 + rr] -= acc;
+      }
     }
     __syncthreads();
   }
@@ -801,20 +868,35 @@ __device__ void denseSolve(Ctx& c, const T* M, T* y) {
   // backward: x_J = Linv_JJ^T y_J, then y_K -= L_JK^T x_J for K < J
   for (int J = Tn - 1; J >= 0; --J) {
     const T* Ajj = M + tileBase(Tn, J, J);
-    if (warp == 0) {
-      T acc = y[J * 32 + lane];
-      for (int row = lane + 1; row < 32; ++row) acc = madT(acc, Ajj[row * kTileLd + lane], y[J * 32 + row]);
-      __syncwarp();
-      y[J * 32 + lane] = acc;
+    T* yJ = y + J * 32;
+    {
+      const int sd = dotSplit(32), w = 32 / sd;
+      T tot = (T)0;
+      int i = 0, p = 0;
+      if ((int)threadIdx.x < 32 * sd) {
+        i = threadIdx.x / sd;
+        p = threadIdx.x % sd;
+        T acc = (T)0;
+        for (int row = p * w; row < (p + 1) * w; ++row)
+          if (row > i) acc = madT(acc, Ajj[row * kTileLd + i], yJ[row]);
+        tot = groupSum(acc, sd);
+      }
+      __syncthreads();
+      if ((int)threadIdx.x < 32 * sd && p == 0) yJ[i] = yJ[i] + tot;
+      __syncthreads();
     }
-    __syncthreads();
     if (J == 0) break;
-    for (int t = threadIdx.x; t < J * 32; t += nth) {
-      const int K = t / 32, cc = t % 32;
+    const int rows = J * 32;
+    const int s = dotSplit(rows), w = 32 / s;
+    for (int t = threadIdx.x; t < rows * s; t += nth) {
+      const int row = t / s, p = t % s;
+      const int K = row / 32, cc = row % 32;
       const T* Ljk = M + tileBase(Tn, J, K);
       T acc = (T)0;
-      for (int row = 0; row < 32; ++row) acc = madT(acc, Ljk[cc * kTileLd + row], y[J * 32 + row]);
-      y[K * 32 + cc] -= acc;
+#pragma unroll 4
+      for (int r2 = p * w; r2 < (p + 1) * w; ++r2) acc = madT(acc, Ljk[cc * kTileLd + r2], yJ[r2]);
+      acc = groupSum(acc, s);
+      if (p == 0) y[K * 32 + cc] -= acc;
     }
     __syncthreads();
   }

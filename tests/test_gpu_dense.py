@@ -78,13 +78,15 @@ def test_dense_ldlt_matches_numpy(arith, nr, nx):
 
 @pytest.mark.parametrize("threads", [64, 128, 256])
 def test_dense_ldlt_block_sizes_agree(threads):
-    """The factor does not depend on the block size (same arithmetic order per entry)."""
+    """The factor does not depend on the block size (same arithmetic order per entry); the solve
+    splits its dot products by block size, so x agrees to rounding."""
     K = quasi_definite(100, 96, seed=3)
     b = np.ones(100)
     ref = probe(K, 96, b, "fp64", threads=256)
     got = probe(K, 96, b, "fp64", threads=threads)
-    for a, r in zip(got[:3], ref[:3]):
-        np.testing.assert_array_equal(a, r)
+    np.testing.assert_array_equal(got[0], ref[0])
+    np.testing.assert_array_equal(got[1], ref[1])
+    assert np.linalg.norm(got[2] - ref[2]) / np.linalg.norm(ref[2]) < 1e-13
 
 
 def test_dense_ldlt_regularized_pivot_rule():
