@@ -1120,6 +1120,14 @@ __device__ __noinline__ double kktSolveImpl(Ctx& c, const DevSettings& st, FactS
       // an FP32 factor whose refinement contracts by less than 4x per step will not reach the
       // tolerance in the remaining steps: go to the high-precision factor now
       if (fp32Factor && !(rel <= st.mixed_fallback_tol) && !(rel <= 0.25 * prev)) break;
+      // a step of the high-precision refinement that does not lower the residual: keep the
+      // better solution and stop (further steps with the same factor do not converge either)
+      if (!fp32Factor && !(rel < prev)) {
+        FOR_T(i, N) sol[i] -= c.cor[i];
+        __syncthreads();
+        rel = prev;
+        break;
+      }
     }
     if (threadIdx.x == 0) c.sc[SC_RSTEPS] += steps;
     const bool mixedFp32 = (sizeof(FT) == 4) && !fs.use64;
