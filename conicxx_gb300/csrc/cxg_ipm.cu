@@ -22,17 +22,29 @@ namespace cxg {
 
 #define FOR_T(i, n) for (int i = (int)threadIdx.x; i < (n); i += (int)blockDim.x)
 
-// sum_{k=beg}^{end-1} val[k] * x[col[k]] with four independent accumulators: one accumulator
-// would make every row a dependent FP64 chain, the cost on GB300's narrow FP64 pipe.
+// sum_{k=beg}^{end-1} val[k] * x[col[k]]: eight loads in flight per round (the values and
+// column indices live in the CTA's scratch, in L2) and four independent accumulators (one would
+// make every row a dependent FP64 chain, the cost on GB300's narrow FP64 pipe).
 __device__ __forceinline__ double csrDot(const double* __restrict__ val, const int* __restrict__ col, int beg, int end,
                                          const double* x) {
   double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
   int k = beg;
-  for (; k + 3 < end; k += 4) {
-    a0 = fma(val[k], x[col[k]], a0);
-    a1 = fma(val[k + 1], x[col[k + 1]], a1);
-    a2 = fma(val[k + 2], x[col[k + 2]], a2);
-    a3 = fma(val[k + 3], x[col[k + 3]], a3);
+  for (; k + 7 < end; k += 8) {
+    double v[8];
+    int ci[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      v[u] = val[k + u];
+      ci[u] = col[k + u];
+    }
+    a0 = fma(v[0], x[ci[0]], a0);
+    a1 = fma(v[1], x[ci[1]], a1);
+    a2 = fma(v[2], x[ci[2]], a2);
+    a3 = fma(v[3], x[ci[3]], a3);
+    a0 = fma(v[4], x[ci[4]], a0);
+    a1 = fma(v[5], x[ci[5]], a1);
+    a2 = fma(v[6], x[ci[6]], a2);
+    a3 = fma(v[7], x[ci[7]], a3);
   }
   for (; k < end; ++k) a0 = fma(val[k], x[col[k]], a0);
   return (a0 + a1) + (a2 + a3);
