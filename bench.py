@@ -284,6 +284,38 @@ def run_gb300(args, rank, world, local_rank):
         import oracle as orc
 
         orc.build()
+        # ---- one instance of n=200, m=300 (Zero^20 x R^160_+ x 40 Q^3): the plain GPU form in
+        # FP64 against the oracle on one host core ----
+        qp0 = generators.config0_qp(0)
+        S0 = Solver()
+        assert S0.setup(qp0, warm_start=0)
+        S0.solve()
+        g_ms = []
+        for _ in range(5):
+            t0_ = time.perf_counter()
+            sol0 = S0.solve()
+            g_ms.append(1e3 * (time.perf_counter() - t0_))
+        S0m = Solver()
+        assert S0m.setup(qp0, warm_start=0, precision=1)
+        S0m.solve()
+        m_ms = []
+        for _ in range(5):
+            t0_ = time.perf_counter()
+            sol0m = S0m.solve()
+            m_ms.append(1e3 * (time.perf_counter() - t0_))
+        O0 = orc.OracleSolver()
+        assert O0.setup(qp0, warm_start=0)
+        O0.solve()
+        c_ms = []
+        for _ in range(5):
+            t0_ = time.perf_counter()
+            _, _, _, oi0 = O0.solve()
+            c_ms.append(1e3 * (time.perf_counter() - t0_))
+        single = {"workload": "n=200, m=300, Zero^20 x R^160_+ x 40 Q^3, one instance, FP64",
+                  "gpu_ms": float(np.median(g_ms)), "gpu_mixed_ms": float(np.median(m_ms)),
+                  "cpu_1core_ms": float(np.median(c_ms)), "iterations_gpu_mixed": int(sol0m.info["iterations"]),
+                  "iterations_gpu": int(sol0.info["iterations"]), "iterations_cpu": int(oi0["iterations"]),
+                  "status_gpu": int(sol0.status), "status_cpu": int(oi0["status"])}
         ncpu = os.cpu_count() or 1
         sample = qps[:args.cpu_sample]
         cpu_wall, cpu_st, _ = orc.batch_solve(sample, ncpu, warm_start=0)
@@ -316,6 +348,7 @@ def run_gb300(args, rank, world, local_rank):
                               "plans + problem values + solutions + results read/written once; the kernel is "
                               "bound by FP64 pipe and barrier latency of the slowest instances, not by HBM"},
             fwd_bwd=fwd_bwd,
+            single_instance=single,
             setup_s=setup_s,
         )
     return ms, wall, clocks, launches_per_step, solved_frac, statuses, result
@@ -331,12 +364,13 @@ def run_reference(args, rank, world):
     if rank != 0:
         return None
     orc.build()
-    qps = generators.contact_batch(COUNT)
+    count = args.count
+    qps = generators.contact_batch(count)
     ncpu = os.cpu_count() or 1
-    sample = args.cpu_sample
+    sample = min(args.cpu_sample, count)
     rates = []
     for i in range(args.warmup + args.steps):
-        lo = (i * sample) % COUNT
+        lo = (i * sample) % count
         sub = qps[lo:lo + sample]
         wall, st, _ = orc.batch_solve(sub, ncpu, warm_start=0)
         if i >= args.warmup:
@@ -346,7 +380,8 @@ def run_reference(args, rank, world):
         "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * sample / value, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded contact generator)",
-        "config": {"workload": WORKLOAD, "count": COUNT, "sample_per_step": sample},
+        "config": {"workload": workload(count), "count_per_gpu": count, "sample_per_step": sample,
+                   "parallelism": "host threads", "warm_start": False},
         "impl": "reference",
         "cpu_baseline": {"value": value, "unit": "solves/s", "cores": ncpu, "kind": "port",
                          "sample": f"{sample} instances per step, one instance per thread, cold start"},

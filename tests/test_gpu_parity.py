@@ -320,3 +320,22 @@ def test_full_size_contact_batch_agrees_with_oracle(oracle_mod, precision):
     errs = np.array(errs)
     print("x error vs oracle: median %.2e p90 %.2e p99 %.2e max %.2e" % (*np.percentile(errs, [50, 90, 99]), errs.max()))
     assert np.mean(errs < 1e-6) >= 0.9 and errs.max() < 1e-4, np.percentile(errs, [50, 90, 99])
+
+
+@pytest.mark.parametrize("precision", [_abi.PRECISION_MIXED, _abi.PRECISION_FP64])
+def test_layer_batch_agrees_with_oracle(oracle_mod, precision):
+    """The 1024-instance differentiable-layer batch (n=100, m=150, Zero^10 x R^100_+ x 10 Q^4)
+    against the oracle: same status on >= 99%, iterations within +-1 on >= 95% of the instances
+    both solve."""
+    _, BatchSolver = _solvers()
+    qps = generators.config3_batch(1024)
+    B = BatchSolver(qps, warm_start=0, precision=precision)
+    _, _, _, infos = B.solve()
+    st, it = infos["status"], infos["iterations"]
+    _, ost, oit = oracle_mod.batch_solve(qps, os.cpu_count() or 1, warm_start=0)
+    agree = st == ost
+    print("layer batch: status agreement %d/%d" % (agree.sum(), len(qps)))
+    assert agree.mean() >= 0.99, (agree.sum(), np.where(~agree)[0][:20])
+    both = agree & (st == 1)
+    d = it[both] - oit[both]
+    assert np.mean(np.abs(d) <= 1) >= 0.95, dict(zip(*np.unique(d, return_counts=True)))
