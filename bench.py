@@ -126,6 +126,7 @@ def run_gb300(args, rank, world, local_rank):
     t0 = time.perf_counter()
     B = BatchSolver(qps, settings=st)
     setup_s = time.perf_counter() - t0
+    tune_report = B.autotune(trials=2) if args.autotune else None
     Px, q, Ax, b = B.concat_values()
     dvals = [torch.from_numpy(v).to(dev) for v in (Px, q, Ax, b)]
     dx = torch.empty(B.n_total, dtype=torch.float64, device=dev)
@@ -351,6 +352,8 @@ def run_gb300(args, rank, world, local_rank):
             single_instance=single,
             setup_s=setup_s,
         )
+    if tune_report is not None:
+        result["autotune"] = tune_report.strip().splitlines()
     return ms, wall, clocks, launches_per_step, solved_frac, statuses, result
 
 
@@ -398,6 +401,8 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=1024)
     ap.add_argument("--plain-instances", type=int, default=16)
     ap.add_argument("--count", type=int, default=COUNT, help="contact instances per GPU")
+    ap.add_argument("--autotune", action="store_true",
+                    help="pick threads per instance for each size bucket by timing (cxg_batch_autotune) before timing")
     ap.add_argument("--entry", default="graph", choices=["graph", "noalloc"],
                     help="graph: the captured concurrent-bucket solve (default); noalloc: the allocation-free "
                          "entry point (direct launches, buckets in sequence)")

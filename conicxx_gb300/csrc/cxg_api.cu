@@ -140,6 +140,7 @@ struct cxg_batch {
   cudaGraphExec_t graphExec = nullptr;
   DevSettings graphSettings{};
   bool graphValid = false;
+  int64_t scratchCapacity = 0;              // doubles allocated in dScratch
   std::vector<DevResult> hRes;
   int lastLaunches = 0;
   double setupTime = 0.0;
@@ -312,6 +313,7 @@ static int buildGroups(cxg_batch* B) {
   B->dScratch = nullptr;
   int rc = devAlloc(&B->dScratch, (size_t)std::max<int64_t>(scratchTotal, 2));
   if (rc) return rc;
+  B->scratchCapacity = std::max<int64_t>(scratchTotal, 2);
   return CXG_OK;
 }
 
@@ -490,6 +492,35 @@ extern "C" int cxg_batch_update_values_device(cxg_batch* B, const double* Px, co
   return copyValues(B, Px, q, Ax, b, cudaMemcpyDeviceToDevice, (cudaStream_t)stream);
 }
 
+// Arguments of one bucket's IPM launch (counter and scratch base given by the caller).
+static LaunchArgs solveArgs(const cxg_batch* B, const Group& g, const DevSettings& ds, int* counter, double* scratch) {
+  LaunchArgs a{};
+  a.desc = B->dDesc;
+  a.order = B->dOrder + g.begin;
+  a.count = g.count;
+  a.counter = counter;
+  a.ipool = B->dIpool;
+  a.dpool = B->dDpool;
+  a.Px = B->dPx;
+  a.q = B->dq;
+  a.Ax = B->dAx;
+  a.b = B->db;
+  a.x = B->dx;
+  a.s = B->ds;
+  a.z = B->dz;
+  a.results = B->dRes;
+  a.warmX = B->dWx;
+  a.warmS = B->dWs;
+  a.warmZ = B->dWz;
+  a.haveWarm = B->dHaveWarm;
+  a.bwd = B->dBwd;
+  a.scratch = scratch;
+  a.scratchStride = g.stride;
+  a.st = ds;
+  a.lay = g.lay;
+  return a;
+}
+
 // Enqueues the device-side solve sequence on `s`: queue resets, then one persistent launch per
 // size bucket, each on its own stream forked from and joined back into `s`, so the buckets run
 // concurrently and the batch waits for its slowest instance once rather than once per bucket.
@@ -512,30 +543,7 @@ static int enqueueSolve(cxg_batch* B, cudaStream_t s) {
     const Group& g = B->groups[gi];
     cudaStream_t gs = (G == 1) ? s : B->groupStreams[gi];
     if (G > 1) CX_CUDA(cudaStreamWaitEvent(gs, B->forkJoin[0], 0));
-    LaunchArgs a{};
-    a.desc = B->dDesc;
-    a.order = B->dOrder + g.begin;
-    a.count = g.count;
-    a.counter = B->dCounters + g.counterIdx;
-    a.ipool = B->dIpool;
-    a.dpool = B->dDpool;
-    a.Px = B->dPx;
-    a.q = B->dq;
-    a.Ax = B->dAx;
-    a.b = B->db;
-    a.x = B->dx;
-    a.s = B->ds;
-    a.z = B->dz;
-    a.results = B->dRes;
-    a.warmX = B->dWx;
-    a.warmS = B->dWs;
-    a.warmZ = B->dWz;
-    a.haveWarm = B->dHaveWarm;
-    a.bwd = B->dBwd;
-    a.scratch = B->dScratch + g.scratchOff;
-    a.scratchStride = g.stride;
-    a.st = ds;
-    a.lay = g.lay;
+    const LaunchArgs a = solveArgs(B, g, ds, B->dCounters + g.counterIdx, B->dScratch + g.scratchOff);
     CX_CUDA(launchIpm(a, g.grid, g.block, g.smem, g.fp32, gs));
     if (G > 1) {
       CX_CUDA(cudaEventRecord(B->forkJoin[gi + 1], gs));
@@ -668,6 +676,103 @@ extern "C" int cxg_batch_describe(const cxg_batch* B, char* buf, int buflen) {
   }
   std::snprintf(buf, (size_t)buflen, "%s", out.c_str());
   return (int)out.size();
+}
+
+// ------------------------------------------------------------------------------------------
+// autotuner: threads per instance for each size bucket, by timing the bucket's launch alone
+// ------------------------------------------------------------------------------------------
+// Resident CTAs of one bucket for a block size (the persistent grid).
+static int bucketGrid(const Group& g, int block, int numSM) {
+  int occ = 0;
+  const cudaError_t oe = ipmOccupancy(&occ, block, g.smem, g.fp32);
+  if (oe != cudaSuccess || occ < 1) occ = 1;
+  return std::max(1, std::min(g.count, occ * numSM));
+}
+
+// Lays the per-bucket scratch regions out again after grids changed; reallocates if it grew.
+static int relayoutScratch(cxg_batch* B) {
+  int64_t total = 0;
+  for (Group& g : B->groups) {
+    g.scratchOff = total;
+    total += g.stride * g.grid;
+  }
+  if (total > B->scratchCapacity) {
+    if (B->dScratch) cudaFree(B->dScratch);
+    B->dScratch = nullptr;
+    B->scratchCapacity = 0;
+    int rc = devAlloc(&B->dScratch, (size_t)std::max<int64_t>(total, 2));
+    if (rc) return rc;
+    B->scratchCapacity = std::max<int64_t>(total, 2);
+  }
+  return CXG_OK;
+}
+
+extern "C" int cxg_batch_autotune(cxg_batch* B, int trials, char* report, int reportLen) {
+  if (!B) return setErr(CXG_E_INVALID, "null batch");
+  if (trials < 1) trials = 1;
+  int numSM = 0;
+  CX_CUDA(cudaDeviceGetAttribute(&numSM, cudaDevAttrMultiProcessorCount, B->device));
+  cxg_settings tst = B->st;
+  tst.warm_start = 0;  // trials leave the warm-start state alone
+  tst.record_timings = 0;
+  const DevSettings ds = makeDevSettings(tst, B->kktSt);
+  static const int kCand[] = {64, 128, 256};
+  std::string rep;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  CX_CUDA(cudaEventCreate(&e0));
+  CX_CUDA(cudaEventCreate(&e1));
+  int rc = CXG_OK;
+  for (size_t gi = 0; gi < B->groups.size() && rc == CXG_OK; ++gi) {
+    Group& g = B->groups[gi];
+    // one trial scratch buffer large enough for the largest candidate grid of this bucket
+    int64_t need = 2;
+    for (int b : kCand) need = std::max<int64_t>(need, g.stride * bucketGrid(g, b, numSM));
+    double* trialScratch = nullptr;
+    if ((rc = devAlloc(&trialScratch, (size_t)need))) break;
+    int bestBlock = g.block;
+    float bestMs = 0.0f;
+    char line[256];
+    std::snprintf(line, sizeof(line), "bucket nr<=%d (%d instances):", g.lay.nrMax, g.count);
+    rep += line;
+    for (int b : kCand) {
+      const int grid = bucketGrid(g, b, numSM);
+      std::vector<float> ms;
+      for (int t = 0; t < trials + 1 && rc == CXG_OK; ++t) {
+        cudaError_t ce = cudaMemsetAsync(B->dCounters + g.counterIdx, 0, sizeof(int), B->stream);
+        if (ce == cudaSuccess) ce = cudaEventRecord(e0, B->stream);
+        const LaunchArgs a = solveArgs(B, g, ds, B->dCounters + g.counterIdx, trialScratch);
+        if (ce == cudaSuccess) ce = launchIpm(a, grid, b, g.smem, g.fp32, B->stream);
+        if (ce == cudaSuccess) ce = cudaEventRecord(e1, B->stream);
+        if (ce == cudaSuccess) ce = cudaEventSynchronize(e1);
+        float v = 0.0f;
+        if (ce == cudaSuccess) ce = cudaEventElapsedTime(&v, e0, e1);
+        if (ce != cudaSuccess) rc = setErr(CXG_E_CUDA, std::string("autotune: ") + cudaGetErrorString(ce));
+        if (t > 0) ms.push_back(v);  // the first run of each shape is a warm-up
+      }
+      if (rc) break;
+      std::sort(ms.begin(), ms.end());
+      const float med = ms[ms.size() / 2];
+      std::snprintf(line, sizeof(line), " %d threads %.3f ms;", b, med);
+      rep += line;
+      if (bestMs == 0.0f || med < bestMs) {
+        bestMs = med;
+        bestBlock = b;
+      }
+    }
+    cudaFree(trialScratch);
+    if (rc) break;
+    g.block = bestBlock;
+    g.grid = bucketGrid(g, bestBlock, numSM);
+    std::snprintf(line, sizeof(line), " -> %d\n", bestBlock);
+    rep += line;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (rc) return rc;
+  if ((rc = relayoutScratch(B))) return rc;
+  B->graphValid = false;  // the captured launch shapes are stale
+  if (report && reportLen > 0) std::snprintf(report, (size_t)reportLen, "%s", rep.c_str());
+  return CXG_OK;
 }
 
 // ------------------------------------------------------------------------------------------

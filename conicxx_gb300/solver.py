@@ -222,6 +222,13 @@ class BatchSolver:
         check(lib().cxg_batch_update_values_device(self._h, Px_ptr, q_ptr, Ax_ptr, b_ptr, stream_ptr),
               "cxg_batch_update_values_device")
 
+    def autotune(self, trials=3):
+        """Pick threads per instance for every size bucket by timing each bucket's launch alone
+        (cxg_batch_autotune); returns the per-bucket report."""
+        buf = C.create_string_buffer(8192)
+        check(lib().cxg_batch_autotune(self._h, int(trials), buf, len(buf)), "cxg_batch_autotune")
+        return buf.value.decode()
+
     def last_launches(self):
         return lib().cxg_batch_last_launches(self._h)
 

@@ -227,6 +227,14 @@ int cxg_batch_backward_device(cxg_batch* batch, const double* dL_dx, double* dq,
 #define CXG_NOALLOC_SCRATCH_BYTES (32ll << 20)
 int cxg_batch_solve_device_noalloc(cxg_batch* batch, double* x, double* s, double* z, cxg_info* info,
                                    void* stream);
+/* Autotuner (no reference counterpart): for every size bucket, times the bucket's persistent
+ * IPM launch alone with 64, 128 and 256 threads per instance (trials timed runs after one
+ * warm-up each, median kept) and keeps the fastest for later solves; grids follow from the
+ * occupancy of the chosen shape and the per-CTA working memory is laid out again. The trials
+ * solve the current values with warm start off and overwrite the last solution (solve again to
+ * read one). Allocates temporary device memory. report (may be NULL) receives one line per
+ * bucket with the measured times. */
+int cxg_batch_autotune(cxg_batch* batch, int trials, char* report, int reportLen);
 /* Kernel launches enqueued by the last solve/backward call of this batch. */
 int cxg_batch_last_launches(const cxg_batch* batch);
 /* Device footprint of the batch in bytes: index plans + equilibration (plan), problem values +

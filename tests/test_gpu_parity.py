@@ -339,3 +339,22 @@ def test_layer_batch_agrees_with_oracle(oracle_mod, precision):
     both = agree & (st == 1)
     d = it[both] - oit[both]
     assert np.mean(np.abs(d) <= 1) >= 0.95, dict(zip(*np.unique(d, return_counts=True)))
+
+
+def test_autotune_keeps_results():
+    """After cxg_batch_autotune picks the launch shapes, a solve gives the same statuses and
+    solutions to solver precision (the dense solves split their dot products by block size, so
+    the last bits may differ)."""
+    _, BatchSolver = _solvers()
+    qps = generators.contact_batch(256, base_seed=5000)
+    B = BatchSolver(qps, warm_start=0)
+    x0, s0, z0, i0 = B.solve()
+    rep = B.autotune(trials=2)
+    assert rep.count("bucket") == len(B.describe().strip().splitlines()), rep
+    x1, s1, z1, i1 = B.solve()
+    same = i0["status"] == i1["status"]
+    assert same.mean() >= 0.99
+    ok = same & (i0["status"] == 1)
+    for i in np.where(ok)[0]:
+        a, b = B.split(x0, s0, z0)[i][0], B.split(x1, s1, z1)[i][0]
+        assert np.max(np.abs(a - b)) <= 1e-5 * max(1.0, np.max(np.abs(b))), i
