@@ -90,6 +90,25 @@ __device__ __forceinline__ df64 dfMad(df64 c, df64 a, df64 b) {
   return df64(h, l);
 }
 
+// Accumulation form of dfMad for long sums (tile products): the exact TwoSum of the high parts
+// is kept, the low-order terms are added in float without renormalising (12 float operations);
+// dfNorm renormalises once at the end. The low part only ever holds rounding terms of the high
+// part's sums, so it stays small relative to it.
+__device__ __forceinline__ df64 dfMadLoose(df64 c, df64 a, df64 b) {
+  const float ph = __fmul_rn(a.hi, b.hi);
+  float pl = __fmaf_rn(a.hi, b.hi, -ph);
+  pl = __fmaf_rn(a.hi, b.lo, pl);
+  pl = __fmaf_rn(a.lo, b.hi, pl);
+  float s, e;
+  dfTwoSum(c.hi, ph, s, e);
+  return df64(s, __fadd_rn(c.lo, __fadd_rn(e, pl)));
+}
+__device__ __forceinline__ df64 dfNorm(df64 c) {
+  float h, l;
+  dfFastTwoSum(c.hi, c.lo, h, l);
+  return df64(h, l);
+}
+
 __device__ __forceinline__ df64& operator+=(df64& a, df64 b) { return a = a + b; }
 __device__ __forceinline__ df64& operator-=(df64& a, df64 b) { return a = a - b; }
 __device__ __forceinline__ df64& operator*=(df64& a, df64 b) { return a = a * b; }

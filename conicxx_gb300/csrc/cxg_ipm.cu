@@ -373,6 +373,13 @@ __device__ __forceinline__ df64 madT(df64 c, df64 a, df64 b) { return dfMad(c, a
 template <typename T>
 __device__ __forceinline__ T msubT(T c, T a, T b) { return c - a * b; }
 __device__ __forceinline__ df64 msubT(df64 c, df64 a, df64 b) { return dfMad(c, -a, b); }
+// Accumulation inside tile products: accT (no renormalisation for double-float), then accEnd.
+template <typename T>
+__device__ __forceinline__ T accT(T c, T a, T b) { return c + a * b; }
+__device__ __forceinline__ df64 accT(df64 c, df64 a, df64 b) { return dfMadLoose(c, a, b); }
+template <typename T>
+__device__ __forceinline__ T accEnd(T c) { return c; }
+__device__ __forceinline__ df64 accEnd(df64 c) { return dfNorm(c); }
 
 // A row of 32 values held in registers (indices are compile-time after unrolling). The
 // double-float row is kept as two float arrays so that it stays in registers.
@@ -394,8 +401,8 @@ struct Row32<df64> {
 
 // 1/d for a pivot. FP32: the IEEE reciprocal intrinsic. FP64 and double-float: Newton-Raphson
 // iteration r <- r + r (1 - d r) from the FP32 reciprocal of the leading part (each step doubles
-// the correct bits: 23 -> 46 -> full), falling back to a division when d is outside the float
-// range or not finite.
+// the correct bits: 23 -> 46 -> full; two steps for FP64, one for double-float), falling back to
+// a division when d is outside the float range or not finite.
 __device__ __forceinline__ float recipT(float d) { return __frcp_rn(d); }
 __device__ __forceinline__ double recipT(double d) {
   const float f = __double2float_rn(d);
@@ -410,9 +417,9 @@ __device__ __forceinline__ double recipT(double d) {
 __device__ __forceinline__ df64 recipT(df64 d) {
   const float af = fabsf(d.hi);
   if (!(af >= 1e-37f && af <= 1e37f)) return df64(1.0f, 0.0f) / d;
-  df64 r(__frcp_rn(d.hi), 0.0f);
+  // one step from the 23-bit seed gives ~46 bits, the double-float rounding level
+  const df64 r(__frcp_rn(d.hi), 0.0f);
   const df64 one(1.0f, 0.0f);
-  r = r + r * (one - d * r);
   return r + r * (one - d * r);
 }
 
@@ -708,15 +715,15 @@ __device__ void tileOffDiag(T* Aij, const T* Ajj) {
 #pragma unroll
       for (int i = 0; i < 4; ++i)
 #pragma unroll
-        for (int j = 0; j < 4; ++j) acc[i][j] = madT(acc[i][j], av[i], cv[j]);
+        for (int j = 0; j < 4; ++j) acc[i][j] = accT(acc[i][j], av[i], cv[j]);
     }
     __syncwarp();
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
       const int col = c0 + j;
-      const T dinv = (T)1 / Ajj[col * kTileLd + col];
+      const T dinv = recipT(Ajj[col * kTileLd + col]);
 #pragma unroll
-      for (int i = 0; i < 4; ++i) Aij[col * kTileLd + lr * 4 + i] = acc[i][j] * dinv;
+      for (int i = 0; i < 4; ++i) Aij[col * kTileLd + lr * 4 + i] = accEnd(acc[i][j]) * dinv;
     }
     __syncwarp();
   }
@@ -745,12 +752,12 @@ __device__ void tileSyrk(T* C, const T* A, const T* B, const T* Ajj) {
 #pragma unroll
       for (int i = 0; i < 4; ++i)
 #pragma unroll
-        for (int j = 0; j < 4; ++j) acc[i][j] = madT(acc[i][j], av[i], bv[j]);
+        for (int j = 0; j < 4; ++j) acc[i][j] = accT(acc[i][j], av[i], bv[j]);
     }
 #pragma unroll
     for (int j = 0; j < 4; ++j)
 #pragma unroll
-      for (int i = 0; i < 4; ++i) C[(c0 + j) * kTileLd + lr * 4 + i] -= acc[i][j];
+      for (int i = 0; i < 4; ++i) C[(c0 + j) * kTileLd + lr * 4 + i] -= accEnd(acc[i][j]);
   }
 }
 
