@@ -594,21 +594,22 @@ __device__ void tileFactorDiagBlocked(T* A, int J, int nr, int nx, const DevSett
 #pragma unroll
         for (int t = 0; t < 8; ++t) {
           const T* Lc = A + (c0 + t) * kTileLd;
-          acc0 = msubT(acc0, u[t], Lc[k]);
-          acc1 = msubT(acc1, u[t], Lc[k + 1]);
-          acc2 = msubT(acc2, u[t], Lc[k + 2]);
-          acc3 = msubT(acc3, u[t], Lc[k + 3]);
+          const T nu = -u[t];
+          acc0 = accT(acc0, nu, Lc[k]);
+          acc1 = accT(acc1, nu, Lc[k + 1]);
+          acc2 = accT(acc2, nu, Lc[k + 2]);
+          acc3 = accT(acc3, nu, Lc[k + 3]);
         }
-        A[k * kTileLd + r] = acc0;
-        A[(k + 1) * kTileLd + r] = acc1;
-        A[(k + 2) * kTileLd + r] = acc2;
-        A[(k + 3) * kTileLd + r] = acc3;
+        A[k * kTileLd + r] = accEnd(acc0);
+        A[(k + 1) * kTileLd + r] = accEnd(acc1);
+        A[(k + 2) * kTileLd + r] = accEnd(acc2);
+        A[(k + 3) * kTileLd + r] = accEnd(acc3);
       }
       for (; k <= r; ++k) {
         T acc = A[k * kTileLd + r];
 #pragma unroll
-        for (int t = 0; t < 8; ++t) acc = msubT(acc, u[t], A[(c0 + t) * kTileLd + k]);
-        A[k * kTileLd + r] = acc;
+        for (int t = 0; t < 8; ++t) acc = accT(acc, -u[t], A[(c0 + t) * kTileLd + k]);
+        A[k * kTileLd + r] = accEnd(acc);
       }
     }
     __syncwarp();
@@ -643,8 +644,8 @@ __device__ void tileFactorDiagBlocked(T* A, int J, int nr, int nx, const DevSett
     for (int i = 0; i < 8; ++i) {
       T acc = (T)0;
 #pragma unroll
-      for (int k = 0; k < i; ++k) acc = madT(acc, A[(o + k) * kTileLd + o + i], y[k]);
-      y[i] = (i < c) ? (T)0 : ((i == c) ? (T)1 : -acc);
+      for (int k = 0; k < i; ++k) acc = accT(acc, A[(o + k) * kTileLd + o + i], y[k]);
+      y[i] = (i < c) ? (T)0 : ((i == c) ? (T)1 : -accEnd(acc));
     }
 #pragma unroll
     for (int i = 0; i < 8; ++i)
@@ -661,10 +662,10 @@ __device__ void tileFactorDiagBlocked(T* A, int J, int nr, int nx, const DevSett
       for (int kk = 8 * Jb; kk < 8 * (Jb + d); kk += 2) {
         const T lv0 = (kk > C) ? A[kk * kTileLd + C] : ((kk == C) ? (T)1 : (T)0);
         const T lv1 = (kk + 1 > C) ? A[(kk + 1) * kTileLd + C] : ((kk + 1 == C) ? (T)1 : (T)0);
-        acc0 = madT(acc0, A[kk * kTileLd + R], lv0);
-        acc1 = madT(acc1, A[(kk + 1) * kTileLd + R], lv1);
+        acc0 = accT(acc0, A[kk * kTileLd + R], lv0);
+        acc1 = accT(acc1, A[(kk + 1) * kTileLd + R], lv1);
       }
-      A[R * kTileLd + C] = acc0 + acc1;
+      A[R * kTileLd + C] = accEnd(acc0) + accEnd(acc1);
     }
     __syncwarp();
     if (r < nb * 8) {
@@ -672,8 +673,8 @@ __device__ void tileFactorDiagBlocked(T* A, int J, int nr, int nx, const DevSett
       const int o = 8 * (Jb + d), C = 8 * Jb + j;
       for (int i = 7; i >= 0; --i) {
         T acc = A[(o + i) * kTileLd + C];
-        for (int i2 = 0; i2 < i; ++i2) acc = madT(acc, A[(o + i) * kTileLd + o + i2], A[(o + i2) * kTileLd + C]);
-        A[(o + i) * kTileLd + C] = -acc;
+        for (int i2 = 0; i2 < i; ++i2) acc = accT(acc, A[(o + i) * kTileLd + o + i2], A[(o + i2) * kTileLd + C]);
+        A[(o + i) * kTileLd + C] = -accEnd(acc);
       }
     }
     __syncwarp();
@@ -856,8 +857,8 @@ __device__ void denseSolve(Ctx& c, const T* M, T* y) {
         i = threadIdx.x / sd;
         p = threadIdx.x % sd;
         T acc = (T)0;
-        for (int col = p * w; col < (p + 1) * w && col < i; ++col) acc = madT(acc, Ajj[i * kTileLd + col], yJ[col]);
-        tot = groupSum(acc, sd);
+        for (int col = p * w; col < (p + 1) * w && col < i; ++col) acc = accT(acc, Ajj[i * kTileLd + col], yJ[col]);
+        tot = groupSum(accEnd(acc), sd);
       }
       __syncthreads();
       if ((int)threadIdx.x < 32 * sd && p == 0) yJ[i] = yJ[i] + tot;
@@ -872,8 +873,8 @@ __device__ void denseSolve(Ctx& c, const T* M, T* y) {
         const T* Lij = M + tileBase(Tn, I, J);
         T acc = (T)0;
 #pragma unroll 4
-        for (int col = p * w; col < (p + 1) * w; ++col) acc = madT(acc, Lij[col * kTileLd + rr], yJ[col]);
-        acc = groupSum(acc, s);
+        for (int col = p * w; col < (p + 1) * w; ++col) acc = accT(acc, Lij[col * kTileLd + rr], yJ[col]);
+        acc = groupSum(accEnd(acc), s);
         if (p == 0) y[I * 32 + rr] -= acc;
       }
     }
@@ -897,8 +898,8 @@ __device__ void denseSolve(Ctx& c, const T* M, T* y) {
         p = threadIdx.x % sd;
         T acc = (T)0;
         for (int row = p * w; row < (p + 1) * w; ++row)
-          if (row > i) acc = madT(acc, Ajj[row * kTileLd + i], yJ[row]);
-        tot = groupSum(acc, sd);
+          if (row > i) acc = accT(acc, Ajj[row * kTileLd + i], yJ[row]);
+        tot = groupSum(accEnd(acc), sd);
       }
       __syncthreads();
       if ((int)threadIdx.x < 32 * sd && p == 0) yJ[i] = yJ[i] + tot;
@@ -913,8 +914,8 @@ __device__ void denseSolve(Ctx& c, const T* M, T* y) {
       const T* Ljk = M + tileBase(Tn, J, K);
       T acc = (T)0;
 #pragma unroll 4
-      for (int r2 = p * w; r2 < (p + 1) * w; ++r2) acc = madT(acc, Ljk[cc * kTileLd + r2], yJ[r2]);
-      acc = groupSum(acc, s);
+      for (int r2 = p * w; r2 < (p + 1) * w; ++r2) acc = accT(acc, Ljk[cc * kTileLd + r2], yJ[r2]);
+      acc = groupSum(accEnd(acc), s);
       if (p == 0) y[K * 32 + cc] -= acc;
     }
     __syncthreads();
