@@ -100,6 +100,8 @@ class Info(C.Structure):
         ("time_dense_solve_s", C.c_double),
         ("time_residual_s", C.c_double),
         ("factor_attempts", C.c_int),
+        ("time_start_s", C.c_double),
+        ("time_end_s", C.c_double),
     ]
 
     def as_dict(self):

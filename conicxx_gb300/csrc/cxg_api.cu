@@ -200,7 +200,8 @@ static int64_t r2(int64_t v) { return (v + 1) & ~int64_t(1); }
 static const int kBucketEdges[] = {32, 64, 96, 128, 160, 192, 256, 384, 512, 1024, 2048, 4096};
 
 static int chooseBlock(int nrMax, int requested) {
-  if (requested == 64 || requested == 128 || requested == 256) return requested;
+  if (requested == 32 || requested == 64 || requested == 128 || requested == 256) return requested;
+  if (nrMax <= 32) return 32;
   if (nrMax <= 64) return 64;
   if (nrMax <= 128) return 128;
   return 256;
@@ -613,6 +614,14 @@ static int fetchInfo(cxg_batch* B, cxg_info* info, double solveTime) {
   }
   CX_CUDA(cudaMemcpy(B->hRes.data(), B->dRes, sizeof(DevResult) * (size_t)B->count, cudaMemcpyDeviceToHost));
   for (int i = 0; i < B->count; ++i) resultToInfo(B->hRes[(size_t)i], info[i], B->setupTime, solveTime);
+  if (B->st.record_timings && B->count > 0) {
+    long long t0 = B->hRes[0].wall_ns[0];
+    for (int i = 1; i < B->count; ++i) t0 = std::min(t0, B->hRes[(size_t)i].wall_ns[0]);
+    for (int i = 0; i < B->count; ++i) {
+      info[i].time_start_s = 1e-9 * (double)(B->hRes[(size_t)i].wall_ns[0] - t0);
+      info[i].time_end_s = 1e-9 * (double)(B->hRes[(size_t)i].wall_ns[1] - t0);
+    }
+  }
   return CXG_OK;
 }
 
@@ -716,7 +725,7 @@ extern "C" int cxg_batch_autotune(cxg_batch* B, int trials, char* report, int re
   tst.warm_start = 0;  // trials leave the warm-start state alone
   tst.record_timings = 0;
   const DevSettings ds = makeDevSettings(tst, B->kktSt);
-  static const int kCand[] = {64, 128, 256};
+  static const int kCand[] = {32, 64, 128, 256};
   std::string rep;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   CX_CUDA(cudaEventCreate(&e0));
@@ -726,7 +735,8 @@ extern "C" int cxg_batch_autotune(cxg_batch* B, int trials, char* report, int re
     Group& g = B->groups[gi];
     // one trial scratch buffer large enough for the largest candidate grid of this bucket
     int64_t need = 2;
-    for (int b : kCand) need = std::max<int64_t>(need, g.stride * bucketGrid(g, b, numSM));
+    for (int b : kCand)
+      if (b >= 64 || g.lay.nrMax <= 64) need = std::max<int64_t>(need, g.stride * bucketGrid(g, b, numSM));
     double* trialScratch = nullptr;
     if ((rc = devAlloc(&trialScratch, (size_t)need))) break;
     int bestBlock = g.block;
@@ -735,6 +745,7 @@ extern "C" int cxg_batch_autotune(cxg_batch* B, int trials, char* report, int re
     std::snprintf(line, sizeof(line), "bucket nr<=%d (%d instances):", g.lay.nrMax, g.count);
     rep += line;
     for (int b : kCand) {
+      if (b < 64 && g.lay.nrMax > 64) continue;  // one warp only for small roots
       const int grid = bucketGrid(g, b, numSM);
       std::vector<float> ms;
       for (int t = 0; t < trials + 1 && rc == CXG_OK; ++t) {

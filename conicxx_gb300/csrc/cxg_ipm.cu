@@ -70,10 +70,19 @@ __device__ __forceinline__ void blockSum(double (&v)[K], double* red) {
 #pragma unroll
     for (int k = 0; k < K; ++k) red[k * 16 + w] = v[k];
   __syncthreads();
+  // pairwise over the warps' partials (depth log2(nw), not nw: FP64 adds are long-latency here)
 #pragma unroll
   for (int k = 0; k < K; ++k) {
-    double t = 0.0;
-    for (int j = 0; j < nw; ++j) t += red[k * 16 + j];
+    const double* r = red + k * 16;
+    double t;
+    if (nw == 1) t = r[0];
+    else if (nw == 2) t = r[0] + r[1];
+    else if (nw == 4) t = (r[0] + r[1]) + (r[2] + r[3]);
+    else if (nw == 8) t = ((r[0] + r[1]) + (r[2] + r[3])) + ((r[4] + r[5]) + (r[6] + r[7]));
+    else {
+      t = 0.0;
+      for (int j = 0; j < nw; ++j) t += r[j];
+    }
     v[k] = t;
   }
 }
@@ -1201,6 +1210,8 @@ __device__ __noinline__ void solveInstance(Ctx& c, const LaunchArgs& a, int inst
   if (threadIdx.x < SC_COUNT) c.sc[threadIdx.x] = 0.0;
   if (threadIdx.x < TM_COUNT) timers(c)[threadIdx.x] = 0;
   const long long tStart = clock64();
+  unsigned long long wallStart = 0;
+  if (st.record_timings && threadIdx.x == 0) asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(wallStart));
   __syncthreads();
 
   const bool useWarm = st.warm_start && a.haveWarm && a.haveWarm[inst];
@@ -1530,6 +1541,12 @@ __device__ __noinline__ void solveInstance(Ctx& c, const LaunchArgs& a, int inst
     R.error_code = 0;
     const long long tot = clock64() - tStart;
     R.cycles[0] = tot;
+    if (st.record_timings) {
+      unsigned long long wallEnd = 0;
+      asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(wallEnd));
+      R.wall_ns[0] = (long long)wallStart;
+      R.wall_ns[1] = (long long)wallEnd;
+    }
     R.cycles[1] = timers(c)[TM_FACTOR];
     R.cycles[2] = timers(c)[TM_SOLVE];
     R.cycles[3] = tot - R.cycles[1] - R.cycles[2];

@@ -126,6 +126,7 @@ struct DevResult {
   int factor_attempts, error_code;  // error_code: 0 ok, else an internal diagnostic (bounds etc.)
   long long cycles[8];              // record_timings: total, factorisation, KKT solves, residual/cones,
                                     // assembly, dense LDL', dense triangular solves, KKT residuals
+  long long wall_ns[2];             // record_timings: device global timer at the instance's start and end
 };
 
 }  // namespace cxg

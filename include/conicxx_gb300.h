@@ -91,8 +91,8 @@ typedef struct cxg_settings {
   double mixed_fallback_tol;  /* relative KKT residual above which an FP32-factor solve is redone
                                  with the high-precision factor: double-float arithmetic (about
                                  48 bits) on the FP32 pipe (default 1e-10) */
-  int threads_per_instance;   /* 0 = by root size (64 up to 64 rows, 128 up to 128, else 256);
-                                 else 64, 128 or 256 */
+  int threads_per_instance;   /* 0 = by root size (32 up to 32 rows, 64 up to 64, 128 up to 128,
+                                 else 256); else 32, 64, 128 or 256 */
   int differentiable;         /* keep each instance's final factorisation, scaling and iterate on the
                                  device so backward() can reuse them (default 0; cxg_solver: 1) */
 } cxg_settings;
@@ -122,6 +122,10 @@ typedef struct cxg_info {
   double time_dense_solve_s;  /* triangular solves with the root factor */
   double time_residual_s;     /* KKT residuals of the refinement */
   int factor_attempts;        /* factorisations attempted (retry ladder and fallback included) */
+  /* with settings.record_timings: when this instance started and finished on the device, in
+     seconds after the earliest start in the batch (batches; 0 for cxg_solver) */
+  double time_start_s;
+  double time_end_s;
 } cxg_info;
 
 /* One problem instance; all pointers are caller-owned host memory (copied, never retained). */
@@ -228,7 +232,7 @@ int cxg_batch_backward_device(cxg_batch* batch, const double* dL_dx, double* dq,
 int cxg_batch_solve_device_noalloc(cxg_batch* batch, double* x, double* s, double* z, cxg_info* info,
                                    void* stream);
 /* Autotuner (no reference counterpart): for every size bucket, times the bucket's persistent
- * IPM launch alone with 64, 128 and 256 threads per instance (trials timed runs after one
+ * IPM launch alone with 32 (roots of at most 64 rows), 64, 128 and 256 threads per instance (trials timed runs after one
  * warm-up each, median kept) and keeps the fastest for later solves; grids follow from the
  * occupancy of the chosen shape and the per-CTA working memory is laid out again. The trials
  * solve the current values with warm start off and overwrite the last solution (solve again to
