@@ -107,6 +107,7 @@ struct Group {
   size_t smem = 0;
   int64_t stride = 0;        // scratch doubles per CTA
   int64_t scratchOff = 0;    // offset of this group's scratch in the batch scratch buffer
+  int occupancy = 1;         // resident CTAs per SM of this bucket's launch shape
   int counterIdx = 0;
 };
 
@@ -303,11 +304,27 @@ static int buildGroups(cxg_batch* B) {
     const cudaError_t oe = ipmOccupancy(&occ, g.block, g.smem, fp32);
     if (oe != cudaSuccess || occ < 1) occ = 1;
     g.grid = std::max(1, std::min(g.count, occ * numSM));
+    g.occupancy = occ;
     g.scratchOff = scratchTotal;
     scratchTotal += g.stride * g.grid;
     g.counterIdx = (int)B->groups.size();
     B->groups.push_back(g);
     s = e;
+  }
+  // Buckets whose CTAs need a whole SM (one resident per SM) run first and would otherwise hold
+  // every SM until their queues drain, so the small-root buckets (many CTAs per SM, cheap in bulk)
+  // would start last and their slowest instances would end the batch. Leave a fifth of the SMs
+  // to the small buckets from the start.
+  bool haveSmall = false;
+  for (const Group& g : B->groups) haveSmall |= g.occupancy > 1;
+  if (haveSmall) {
+    const int cap = std::max(1, numSM - numSM / 5);
+    scratchTotal = 0;
+    for (Group& g : B->groups) {
+      if (g.occupancy == 1) g.grid = std::min(g.grid, cap);
+      g.scratchOff = scratchTotal;
+      scratchTotal += g.stride * g.grid;
+    }
   }
   // scratch
   if (B->dScratch) cudaFree(B->dScratch);
@@ -540,7 +557,17 @@ static int enqueueSolve(cxg_batch* B, cudaStream_t s) {
     B->forkJoin.push_back(e);
   }
   CX_CUDA(cudaEventRecord(B->forkJoin[0], s));
-  for (size_t gi = 0; gi < G; ++gi) {
+  // Launch order: the largest-root bucket first (its slowest instances are the longest), then the
+  // buckets with several CTAs per SM (cheap in bulk; they take the SMs the large buckets leave
+  // free), then the remaining whole-SM buckets.
+  std::vector<size_t> launchOrder;
+  launchOrder.reserve(G);
+  if (G > 0) launchOrder.push_back(0);
+  for (size_t gi = 1; gi < G; ++gi)
+    if (B->groups[gi].occupancy > 1) launchOrder.push_back(gi);
+  for (size_t gi = 1; gi < G; ++gi)
+    if (B->groups[gi].occupancy <= 1) launchOrder.push_back(gi);
+  for (size_t gi : launchOrder) {
     const Group& g = B->groups[gi];
     cudaStream_t gs = (G == 1) ? s : B->groupStreams[gi];
     if (G > 1) CX_CUDA(cudaStreamWaitEvent(gs, B->forkJoin[0], 0));
@@ -916,7 +943,17 @@ static int enqueueAdjoint(cxg_batch* B, cudaStream_t s, const double* gx, double
   CX_CUDA(cudaMemsetAsync(B->dCounters, 0, sizeof(int) * (B->groups.size() + 1), s));
   const size_t G = B->groups.size();
   CX_CUDA(cudaEventRecord(B->forkJoin[0], s));
-  for (size_t gi = 0; gi < G; ++gi) {
+  // Launch order: the largest-root bucket first (its slowest instances are the longest), then the
+  // buckets with several CTAs per SM (cheap in bulk; they take the SMs the large buckets leave
+  // free), then the remaining whole-SM buckets.
+  std::vector<size_t> launchOrder;
+  launchOrder.reserve(G);
+  if (G > 0) launchOrder.push_back(0);
+  for (size_t gi = 1; gi < G; ++gi)
+    if (B->groups[gi].occupancy > 1) launchOrder.push_back(gi);
+  for (size_t gi = 1; gi < G; ++gi)
+    if (B->groups[gi].occupancy <= 1) launchOrder.push_back(gi);
+  for (size_t gi : launchOrder) {
     const Group& g = B->groups[gi];
     cudaStream_t gs = (G == 1) ? s : B->groupStreams[gi];
     if (G > 1) CX_CUDA(cudaStreamWaitEvent(gs, B->forkJoin[0], 0));

@@ -1609,8 +1609,11 @@ __device__ void setupCtx(Ctx& c, const LaunchArgs& a, int inst, unsigned char* s
 // ------------------------------------------------------------------------------------------
 // kernel: persistent CTAs over an atomic instance queue
 // ------------------------------------------------------------------------------------------
-template <typename FT>
-__global__ void __launch_bounds__(256) ipmKernel(LaunchArgs a) {
+// kMaxThreads / kMinBlocks: the large-root form (up to 256 threads, registers for one CTA per
+// SM) and the small-root form (up to 64 threads, at least 8 CTAs per SM: small instances are
+// bound by FP64 latency, so more of them resident per SM is more throughput).
+template <typename FT, int kMaxThreads, int kMinBlocks>
+__global__ void __launch_bounds__(kMaxThreads, kMinBlocks) ipmKernel(LaunchArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ int sInst;
   __shared__ int sRedi[4];
@@ -1717,30 +1720,27 @@ cudaError_t launchAdjoint(const LaunchArgs& a, int grid, int block, size_t smem,
   return cudaGetLastError();
 }
 
-// explicit instantiations through the host launchers
+// explicit instantiations through the host launchers: the small-root form for blocks of up to
+// 64 threads, the large-root form otherwise
+using IpmFn = void (*)(LaunchArgs);
+static IpmFn ipmFor(bool fp32, int block) {
+  if (block <= 64) return fp32 ? ipmKernel<float, 64, 8> : ipmKernel<double, 64, 8>;
+  return fp32 ? ipmKernel<float, 256, 1> : ipmKernel<double, 256, 1>;
+}
+
 cudaError_t launchIpm(const LaunchArgs& a, int grid, int block, size_t smem, bool fp32, cudaStream_t stream) {
-  if (fp32) {
-    cudaError_t e = cudaFuncSetAttribute(ipmKernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    ipmKernel<float><<<grid, block, smem, stream>>>(a);
-  } else {
-    cudaError_t e = cudaFuncSetAttribute(ipmKernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    ipmKernel<double><<<grid, block, smem, stream>>>(a);
-  }
+  const IpmFn k = ipmFor(fp32, block);
+  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  k<<<grid, block, smem, stream>>>(a);
   return cudaGetLastError();
 }
 
 cudaError_t ipmOccupancy(int* blocksPerSM, int block, size_t smem, bool fp32) {
-  cudaError_t e;
-  if (fp32) {
-    e = cudaFuncSetAttribute(ipmKernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocksPerSM, ipmKernel<float>, block, smem);
-  }
-  e = cudaFuncSetAttribute(ipmKernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  const IpmFn k = ipmFor(fp32, block);
+  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocksPerSM, ipmKernel<double>, block, smem);
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocksPerSM, k, block, smem);
 }
 
 }  // namespace cxg
