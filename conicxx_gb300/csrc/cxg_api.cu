@@ -13,6 +13,8 @@
 #include <cstdio>
 #include <cstring>
 #include <mutex>
+#include <stdexcept>
+#include <thread>
 #include <numeric>
 #include <string>
 #include <vector>
@@ -410,9 +412,33 @@ extern "C" int cxg_batch_create(cxg_batch** out, int count, const cxg_problem* p
   B->st = st;
   B->kktSt = st;
   try {
+    // Host planning, the set-up cost when contact patterns change: contiguous chunks of instances
+    // are planned on worker threads into their own pools, then appended in instance order.
+    const int hw = (int)std::max(1u, std::thread::hardware_concurrency());
+    const int nth = std::max(1, std::min({hw, 32, count / 16}));
+    std::vector<Pools> part((size_t)nth);
+    std::vector<std::string> fail((size_t)nth);
+    auto work = [&](int t) {
+      const int lo = (int)((int64_t)count * t / nth), hi = (int)((int64_t)count * (t + 1) / nth);
+      try {
+        for (int i = lo; i < hi; ++i) planInstance(problems[i], st, part[(size_t)t]);
+      } catch (const std::exception& ex) {
+        fail[(size_t)t] = ex.what();
+      }
+    };
+    if (nth == 1) {
+      work(0);
+    } else {
+      std::vector<std::thread> pool;
+      pool.reserve((size_t)nth);
+      for (int t = 0; t < nth; ++t) pool.emplace_back(work, t);
+      for (std::thread& th : pool) th.join();
+    }
+    for (int t = 0; t < nth; ++t)
+      if (!fail[(size_t)t].empty()) throw std::runtime_error(fail[(size_t)t]);
+    for (const Pools& pp : part) appendPools(B->pools, pp);
     for (int i = 0; i < count; ++i) {
       const cxg_problem& pr = problems[i];
-      planInstance(pr, st, B->pools);
       B->Pp.emplace_back(pr.Pp, pr.Pp + pr.n + 1);
       B->Pi.emplace_back(pr.Pi, pr.Pi + pr.Pp[pr.n]);
       B->Ap.emplace_back(pr.Ap, pr.Ap + pr.n + 1);

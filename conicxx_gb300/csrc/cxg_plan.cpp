@@ -277,4 +277,30 @@ void planInstance(const cxg_problem& pr, const cxg_settings& st, Pools& pools) {
   pools.desc.push_back(D);
 }
 
+void appendPools(Pools& dst, const Pools& src) {
+  const int64_t ib = (int64_t)dst.ipool.size(), db = (int64_t)dst.dpool.size();
+  dst.ipool.insert(dst.ipool.end(), src.ipool.begin(), src.ipool.end());
+  dst.dpool.insert(dst.dpool.end(), src.dpool.begin(), src.dpool.end());
+  for (InstanceDesc D : src.desc) {
+    for (int64_t* f : {&D.iPp, &D.iPi, &D.iPsRow, &D.iPsCol, &D.iPsSrc, &D.iPdiag, &D.iPlowIdx, &D.iPlowSrc, &D.iAp,
+                       &D.iAi, &D.iArRow, &D.iArCol, &D.iArSrc, &D.iAZIdx, &D.iAZSrc, &D.iSocOff, &D.iSocDim,
+                       &D.iUnitAd, &D.iUnitSup, &D.iSup, &D.iAdSrc, &D.iTgtIdx, &D.iTgtBeg, &D.iContrib})
+      *f += ib;
+    D.dD += db;
+    D.dE += db;
+    D.vPx += dst.totPx;
+    D.vQ += dst.totQ;
+    D.vAx += dst.totAx;
+    D.vB += dst.totB;
+    D.vX = D.vQ;
+    D.vS = D.vB;
+    D.vZ = D.vB;
+    dst.desc.push_back(D);
+  }
+  dst.totPx += src.totPx;
+  dst.totQ += src.totQ;
+  dst.totAx += src.totAx;
+  dst.totB += src.totB;
+}
+
 }  // namespace cxg

@@ -30,6 +30,10 @@ void computeEquilibration(const cxg_problem& pr, const cxg_settings& st, std::ve
 // Appends the plan of `pr` to `pools` (values are NOT copied; see packValues).
 void planInstance(const cxg_problem& pr, const cxg_settings& st, Pools& pools);
 
+// Appends the plans of `src` (planned on their own) to `dst`, shifting every pool and value
+// offset of src's instances by what dst already holds.
+void appendPools(Pools& dst, const Pools& src);
+
 // Whether P's upper-CSC pattern / A's CSC pattern equal the instance's (updateData check,
 // kkt_system.cpp:10-19).
 bool samePattern(const std::vector<int>& p_ref, const std::vector<int>& i_ref, int cols,
