@@ -38,14 +38,17 @@ def _need_gpu():
 
 
 # ---- reference known-answer tests ------------------------------------------------------------
+@pytest.mark.parametrize("linear_solver", [_abi.LINSOLVER_EIGEN, _abi.LINSOLVER_QDLDL, _abi.LINSOLVER_REGULARIZED])
 @pytest.mark.parametrize("precision", [_abi.PRECISION_FP64, _abi.PRECISION_MIXED])
 @pytest.mark.parametrize("idx", range(8))
-def test_kats(kats, idx, precision):
+def test_kats(kats, idx, precision, linear_solver):
+    """Every known-answer problem, in both precisions and with each LinearSolverBackend value
+    (the reference runs its KKT tests over all three, test/kkt/test_kkt_system_backends.cpp:32-135)."""
     Solver, _ = _solvers()
     k = kats[idx]
     qp = kat_qp(k)
     S = Solver()
-    assert S.setup(qp, precision=precision)
+    assert S.setup(qp, precision=precision, linear_solver=linear_solver)
     sol = S.solve()
     assert sol.status == k["status"], (k["name"], sol.status_name)
     if k["x"] is not None:
@@ -376,3 +379,23 @@ def test_larger_instance_root_in_scratch(oracle_mod, precision):
     assert sol.status == io["status"] == 1
     assert abs(sol.info["iterations"] - io["iterations"]) <= 1
     assert np.max(np.abs(sol.x - xo)) <= 1e-6 * max(1.0, np.max(np.abs(xo)))
+
+
+@pytest.mark.parametrize("linear_solver", [_abi.LINSOLVER_QDLDL, _abi.LINSOLVER_REGULARIZED])
+@pytest.mark.parametrize("precision", [_abi.PRECISION_FP64, _abi.PRECISION_MIXED])
+def test_rank_deficient_equalities_stay_finite(oracle_mod, precision, linear_solver):
+    """A rank-deficient Zero-cone block (two identical equality rows, the case of
+    test/kkt/test_kkt_system.cpp:137-158) inside a full solve: regularisation keeps every KKT solve
+    finite, and the consistent system is Solved as by the oracle."""
+    from conicxx_gb300 import Solver
+    from conicxx_gb300.problem import QP, Csc
+
+    P = Csc.from_triplets(3, 3, [(0, 0, 1.0), (1, 1, 1.0), (2, 2, 1.0)])
+    A = Csc.from_triplets(4, 3, [(0, 0, 1.0), (0, 1, 1.0), (1, 0, 1.0), (1, 1, 1.0), (2, 2, -1.0), (3, 0, -1.0)])
+    qp = QP(P, np.array([-1.0, 0.5, 0.2]), A, np.array([1.0, 1.0, 0.0, 0.0]), 2, 2, [])
+    S = Solver()
+    assert S.setup(qp, precision=precision, linear_solver=linear_solver)
+    sol = S.solve()
+    xo, _, _, io, _ = oracle_mod.solve(qp, linear_solver=linear_solver)
+    assert sol.status == io["status"] == _abi.STATUS_SOLVED
+    assert np.all(np.isfinite(sol.x)) and np.allclose(sol.x, xo, atol=1e-6)
