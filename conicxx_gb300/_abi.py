@@ -55,6 +55,7 @@ class Settings(C.Structure):
         ("mixed_fallback_tol", C.c_double),
         ("threads_per_instance", C.c_int),
         ("differentiable", C.c_int),
+        ("whole_gpu_root", C.c_int),
     ]
 
 
@@ -68,6 +69,7 @@ def default_settings(**overrides):
         warm_start=1, verbose=0, record_timings=0, validate_inputs=1,
         linear_solver=LINSOLVER_QDLDL, precision=PRECISION_FP64, mixed_refine_max_iter=4,
         mixed_fallback_tol=1e-10, threads_per_instance=0, differentiable=0,
+        whole_gpu_root=0,
     )
     for k, v in overrides.items():
         if not hasattr(s, k):

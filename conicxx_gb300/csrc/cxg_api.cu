@@ -96,6 +96,8 @@ extern "C" void cxg_default_settings(cxg_settings* s) {
   s->mixed_refine_max_iter = 4;
   s->mixed_fallback_tol = 1e-10;
   s->threads_per_instance = 0;
+  s->differentiable = 0;
+  s->whole_gpu_root = 0;
 }
 
 // ------------------------------------------------------------------------------------------
@@ -148,12 +150,14 @@ struct cxg_batch {
   int lastLaunches = 0;
   double setupTime = 0.0;
   int device = 0;
+  bool gridMode = false;                    // one instance, root spread over every SM (launchIpmGrid)
+  void* dGridCtl = nullptr;                 // its control block
 
   ~cxg_batch() {
     if (graphExec) cudaGraphExecDestroy(graphExec);
     if (graph) cudaGraphDestroy(graph);
     void* ptrs[] = {dDesc, dIpool, dDpool, dPx, dq, dAx, db, dx, ds, dz, dRes, dWx, dWs, dWz, dHaveWarm, dScratch,
-                    dCounters, dOrder, dBwd, dGx, dGq, dGb, dGP, dGA};
+                    dCounters, dOrder, dBwd, dGx, dGq, dGb, dGP, dGA, dGridCtl};
     for (void* p : ptrs)
       if (p) cudaFree(p);
     for (cudaEvent_t e : forkJoin) cudaEventDestroy(e);
@@ -201,6 +205,12 @@ static int64_t r2(int64_t v) { return (v + 1) & ~int64_t(1); }
 // Group boundaries on the root dimension nr; each group gets a shared-memory layout sized for
 // its largest instance.
 static const int kBucketEdges[] = {32, 64, 96, 128, 160, 192, 256, 384, 512, 1024, 2048, 4096};
+// Root sizes: largest one-CTA root; a single instance above kGridAutoRoot rows takes the
+// whole-GPU root (whole_gpu_root = 0), which accepts up to kGridMaxRoot rows (a 70 GB FP64 root).
+static const int kCtaMaxRoot = 4096;
+static const int kGridAutoRoot = 512;
+static const int kGridMaxRoot = 131072;
+static const int kGridMaxAdjointRoot = 8192;
 
 static int chooseBlock(int nrMax, int requested) {
   if (requested == 32 || requested == 64 || requested == 128 || requested == 256) return requested;
@@ -213,6 +223,7 @@ static int chooseBlock(int nrMax, int requested) {
 static int buildGroups(cxg_batch* B) {
   const int N = B->count;
   const bool fp32 = B->st.precision == CXG_PRECISION_MIXED;
+  const bool gridMode = B->gridMode;
   int dev = 0;
   CX_CUDA(cudaGetDevice(&dev));
   B->device = dev;
@@ -262,7 +273,8 @@ static int buildGroups(cxg_batch* B) {
     const int64_t budget = (int64_t)smemOptin - (int64_t)fixedSmem;
     L.redOff = 0;
     L.vecOff = redBytes;
-    L.vecInSmem = (redBytes + vecBytes <= budget) ? 1 : 0;
+    // whole-GPU form: everything the other CTAs read (vectors, root, solve vector) in scratch
+    L.vecInSmem = (!gridMode && redBytes + vecBytes <= budget) ? 1 : 0;
     int64_t used = redBytes + (L.vecInSmem ? vecBytes : 0);
     used = (used + 15) & ~int64_t(15);
     L.rootOff = used;
@@ -270,17 +282,17 @@ static int buildGroups(cxg_batch* B) {
     // the FP32 root then shares that region.
     L.rootInSmem = 0;
     L.root64InSmem = 0;
-    if (used + root64Bytes <= budget) {
+    if (!gridMode && used + root64Bytes <= budget) {
       L.rootInSmem = 1;
       L.root64InSmem = 1;
       used += root64Bytes;
-    } else if (fp32 && used + root32Bytes <= budget) {
+    } else if (!gridMode && fp32 && used + root32Bytes <= budget) {
       L.rootInSmem = 1;
       used += root32Bytes;
     }
     L.total = used;
     g.smem = (size_t)used;
-    g.block = chooseBlock(L.nrMax, B->st.threads_per_instance);
+    g.block = gridMode ? 256 : chooseBlock(L.nrMax, B->st.threads_per_instance);
     // per-instance scratch layout (relative to the CTA base); the FP64 root is needed when the
     // root is not in shared memory (FP64 precision) or for the mixed-precision fallback.
     const bool needRoot64 = !L.root64InSmem;
@@ -303,12 +315,22 @@ static int buildGroups(cxg_batch* B) {
     g.stride = std::max<int64_t>(r2(stride), 2);
     // persistent grid: resident CTAs for this configuration, capped by the group size
     int occ = 0;
-    const cudaError_t oe = ipmOccupancy(&occ, g.block, g.smem, fp32);
-    if (oe != cudaSuccess || occ < 1) occ = 1;
-    g.grid = std::max(1, std::min(g.count, occ * numSM));
-    g.occupancy = occ;
-    g.scratchOff = scratchTotal;
-    scratchTotal += g.stride * g.grid;
+    if (gridMode) {
+      // cooperative launch: every CTA resident; only CTA 0 holds an instance (and scratch)
+      CX_CUDA(ipmGridOccupancy(&occ, g.smem, fp32));
+      if (occ * numSM < 2) return setErr(CXG_E_UNSUPPORTED, "the whole-GPU root needs two resident CTAs");
+      g.grid = occ * numSM;
+      g.occupancy = 1;
+      g.scratchOff = scratchTotal;
+      scratchTotal += g.stride;
+    } else {
+      const cudaError_t oe = ipmOccupancy(&occ, g.block, g.smem, fp32);
+      if (oe != cudaSuccess || occ < 1) occ = 1;
+      g.grid = std::max(1, std::min(g.count, occ * numSM));
+      g.occupancy = occ;
+      g.scratchOff = scratchTotal;
+      scratchTotal += g.stride * g.grid;
+    }
     g.counterIdx = (int)B->groups.size();
     B->groups.push_back(g);
     s = e;
@@ -357,6 +379,7 @@ static int uploadPlan(cxg_batch* B) {
   if ((rc = devAlloc(&B->dHaveWarm, N))) return rc;
   if ((rc = devAlloc(&B->dCounters, B->groups.size() + 1))) return rc;
   if ((rc = devAlloc(&B->dOrder, N))) return rc;
+  if (B->gridMode && (rc = devAlloc(reinterpret_cast<unsigned char**>(&B->dGridCtl), gridCtlBytes()))) return rc;
   if (B->st.differentiable) {
     if ((rc = devAlloc(&B->dBwd, (size_t)B->bwdTotal))) return rc;
     if ((rc = devAlloc(&B->dGx, (size_t)B->pools.totQ))) return rc;
@@ -402,15 +425,26 @@ extern "C" int cxg_batch_create(cxg_batch** out, int count, const cxg_problem* p
     if (e.empty()) e = checkFinite(pr.q, pr.n, "q");
     if (e.empty()) e = checkFinite(pr.b, pr.m, "b");
     if (!e.empty()) return setErr(CXG_E_INVALID, "instance " + std::to_string(i) + ": " + e);
-    if (pr.n + pr.zero_dim > 4096)
-      return setErr(CXG_E_UNSUPPORTED, "instance " + std::to_string(i) +
-                                           ": n + zero_dim > 4096 exceeds the single-CTA device path");
+    const int nr = pr.n + pr.zero_dim;
+    if (nr > kCtaMaxRoot && !(count == 1 && st.whole_gpu_root >= 0 && nr <= kGridMaxRoot))
+      return setErr(CXG_E_UNSUPPORTED,
+                    "instance " + std::to_string(i) + ": n + zero_dim = " + std::to_string(nr) +
+                        " exceeds the one-CTA root (4096 rows); a single instance (count 1, whole_gpu_root >= 0) "
+                        "takes the whole-GPU root up to 131072 rows");
   }
+  // One instance with a root beyond what one SM factors quickly: spread the root over every SM.
+  const int nr0 = problems[0].n + problems[0].zero_dim;
+  const bool gridMode = count == 1 && (st.whole_gpu_root == 1 || (st.whole_gpu_root == 0 && nr0 > kGridAutoRoot) ||
+                                       nr0 > kCtaMaxRoot);
+  // the adjoint keeps an FP64 copy of the final factor and solves with it on one CTA: offered up
+  // to 8192 root rows
+  if (gridMode && nr0 > kGridMaxAdjointRoot) st.differentiable = 0;
   cxg_batch* B = new (std::nothrow) cxg_batch();
   if (!B) return setErr(CXG_E_NOMEM, "host allocation failed");
   B->count = count;
   B->st = st;
   B->kktSt = st;
+  B->gridMode = gridMode;
   try {
     // Host planning, the set-up cost when contact patterns change: contiguous chunks of instances
     // are planned on worker threads into their own pools, then appended in instance order.
@@ -582,6 +616,14 @@ static int enqueueSolve(cxg_batch* B, cudaStream_t s) {
     CX_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     B->forkJoin.push_back(e);
   }
+  if (B->gridMode) {
+    const Group& g = B->groups[0];
+    CX_CUDA(cudaMemsetAsync(B->dGridCtl, 0, gridCtlBytes(), s));
+    const LaunchArgs a = solveArgs(B, g, ds, B->dCounters, B->dScratch + g.scratchOff);
+    CX_CUDA(launchIpmGrid(a, reinterpret_cast<GridCtl*>(B->dGridCtl), g.grid, g.smem, g.fp32, s));
+    B->lastLaunches = 1;
+    return CXG_OK;
+  }
   CX_CUDA(cudaEventRecord(B->forkJoin[0], s));
   // Launch order: the largest-root bucket first (its slowest instances are the longest), then the
   // buckets with several CTAs per SM (cheap in bulk; they take the SMs the large buckets leave
@@ -610,6 +652,8 @@ static int enqueueSolve(cxg_batch* B, cudaStream_t s) {
 
 // Device-side solve through the captured graph (re-captured when the settings change).
 static int runSolve(cxg_batch* B, cudaStream_t s) {
+  // the whole-GPU form is one cooperative launch: enqueued directly, not through a graph
+  if (B->gridMode) return enqueueSolve(B, s);
   const DevSettings ds = makeDevSettings(B->st, B->kktSt);
   if (!B->graphValid || !sameDev(ds, B->graphSettings)) {
     if (B->graphExec) { cudaGraphExecDestroy(B->graphExec); B->graphExec = nullptr; }
@@ -731,9 +775,9 @@ extern "C" int cxg_batch_describe(const cxg_batch* B, char* buf, int buflen) {
     char line[512];
     std::snprintf(line, sizeof(line),
                   "group instances=%d nrMax=%d nMax=%d mMax=%d %s block=%d grid=%d smem=%zu vecInSmem=%d "
-                  "rootInSmem=%d root64InSmem=%d scratchPerCTA=%lld\n",
+                  "rootInSmem=%d root64InSmem=%d scratchPerCTA=%lld wholeGPU=%d\n",
                   g.count, g.lay.nrMax, g.lay.nMax, g.lay.mMax, g.fp32 ? "mixed" : "fp64", g.block, g.grid, g.smem,
-                  g.lay.vecInSmem, g.lay.rootInSmem, g.lay.root64InSmem, (long long)g.stride);
+                  g.lay.vecInSmem, g.lay.rootInSmem, g.lay.root64InSmem, (long long)g.stride, B->gridMode ? 1 : 0);
     out += line;
   }
   std::snprintf(buf, (size_t)buflen, "%s", out.c_str());
@@ -771,6 +815,10 @@ static int relayoutScratch(cxg_batch* B) {
 
 extern "C" int cxg_batch_autotune(cxg_batch* B, int trials, char* report, int reportLen) {
   if (!B) return setErr(CXG_E_INVALID, "null batch");
+  if (B->gridMode) {  // one launch shape: a CTA of 256 threads on every SM
+    if (report && reportLen > 0) std::snprintf(report, (size_t)reportLen, "whole-GPU root: nothing to tune\n");
+    return CXG_OK;
+  }
   if (trials < 1) trials = 1;
   int numSM = 0;
   CX_CUDA(cudaDeviceGetAttribute(&numSM, cudaDevAttrMultiProcessorCount, B->device));
@@ -1004,7 +1052,8 @@ static int enqueueAdjoint(cxg_batch* B, cudaStream_t s, const double* gx, double
     a.scratchStride = g.stride;
     a.st = ds;
     a.lay = g.lay;
-    CX_CUDA(launchAdjoint(a, g.grid, g.block, g.smem, gs));
+    // whole-GPU form: the single instance and its scratch belong to CTA 0 (one CTA)
+    CX_CUDA(launchAdjoint(a, B->gridMode ? 1 : g.grid, g.block, g.smem, gs));
     if (G > 1) {
       CX_CUDA(cudaEventRecord(B->forkJoin[gi + 1], gs));
       CX_CUDA(cudaStreamWaitEvent(s, B->forkJoin[gi + 1], 0));
@@ -1081,6 +1130,7 @@ static int noallocArena(int dev, unsigned char** out) {
 extern "C" int cxg_batch_solve_device_noalloc(cxg_batch* B, double* x, double* s, double* z, cxg_info* info,
                                               void* stream) {
   if (!B) return setErr(CXG_E_INVALID, "null batch");
+  if (B->gridMode) return setErr(CXG_E_UNSUPPORTED, "the whole-GPU root of a single large instance has its own scratch");
   int dev = -1;
   CX_CUDA(cudaGetDevice(&dev));
   if (dev != B->device) return setErr(CXG_E_INVALID, "the batch lives on another device: make that device current");

@@ -201,8 +201,9 @@ extern "C" int cxg_equilibration(const cxg_problem* pr, const cxg_settings* st, 
 extern "C" int cxg_dense_ldlt(int nr, int nx, const double* K, const double* b, int arith, int threads,
                               int linear_solver, double* L, double* D, double* x, long long* cycles, int* flags) {
   using namespace cxg;
-  if (nr < 1 || nx < 0 || nx > nr || !K || !b || arith < 0 || arith > 2 || threads < 32 || threads > 256 ||
-      (threads % 32) != 0) {
+  const bool whole = threads == -1;
+  if (nr < 1 || nx < 0 || nx > nr || !K || !b || arith < 0 || arith > 2 ||
+      (!whole && (threads < 32 || threads > 256 || (threads % 32) != 0))) {
     lastErrorRef() = "cxg_dense_ldlt: bad arguments";
     return CXG_E_INVALID;
   }
@@ -210,7 +211,7 @@ extern "C" int cxg_dense_ldlt(int nr, int nx, const double* K, const double* b, 
   int dev = 0, optin = 0;
   DG_CUDA(cudaGetDevice(&dev));
   DG_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
-  if (denseProbeSmem(arith, nr) + 2048 > (size_t)optin) {
+  if (!whole && denseProbeSmem(arith, nr) + 2048 > (size_t)optin) {
     lastErrorRef() = "cxg_dense_ldlt: matrix too large for one CTA's shared memory";
     return CXG_E_UNSUPPORTED;
   }
@@ -233,7 +234,7 @@ extern "C" int cxg_dense_ldlt(int nr, int nx, const double* K, const double* b, 
   double* dD = (double*)alloc((size_t)nr * 8);
   double* dX = (double*)alloc((size_t)nr * 8);
   long long* dC = (long long*)alloc(2 * sizeof(long long));
-  int* dF = (int*)alloc(2 * sizeof(int));
+  int* dF = (int*)alloc(3 * sizeof(int));
   if (bufs.size() != 7) {
     for (void* p : bufs) cudaFree(p);
     lastErrorRef() = "cxg_dense_ldlt: device allocation failed";
@@ -247,7 +248,7 @@ extern "C" int cxg_dense_ldlt(int nr, int nx, const double* K, const double* b, 
   if (D) DG_CUDA(cudaMemcpy(D, dD, (size_t)nr * 8, cudaMemcpyDeviceToHost));
   if (x) DG_CUDA(cudaMemcpy(x, dX, (size_t)nr * 8, cudaMemcpyDeviceToHost));
   if (cycles) DG_CUDA(cudaMemcpy(cycles, dC, 2 * sizeof(long long), cudaMemcpyDeviceToHost));
-  if (flags) DG_CUDA(cudaMemcpy(flags, dF, 2 * sizeof(int), cudaMemcpyDeviceToHost));
+  if (flags) DG_CUDA(cudaMemcpy(flags, dF, (whole ? 3 : 2) * sizeof(int), cudaMemcpyDeviceToHost));
   for (void* p : bufs) cudaFree(p);
   return CXG_OK;
 }

@@ -1,4 +1,5 @@
-// The interior-point hot path on the GPU: one CTA runs the complete homogeneous self-dual
+// The interior-point hot path on the GPU (device code; instantiated by cxg_ipm_f32.cu,
+// cxg_ipm_f64.cu and cxg_ipm_probe.cu, which compile in parallel): one CTA runs the complete homogeneous self-dual
 // embedding IPM of ConicXX (src/conicxx/solver_impl.cpp:220-560 as numbered in that file's
 // SolverImpl::solve and helpers) for one instance at a time, taking instances from an atomic
 // work queue (persistent CTAs, heaviest instances first). All iterates live in shared memory;
@@ -9,6 +10,8 @@
 // solve whose FP64-refined relative residual stays above mixed_fallback_tol (or is not finite),
 // or whose FP32 factor has a pivot of the wrong sign, switches that instance to an FP64 factor
 // for the rest of its solve ("sticky" fallback; counted in DevResult::fp64_fallbacks).
+#pragma once
+
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdint.h>
@@ -111,6 +114,8 @@ __device__ __forceinline__ int blockOrInt(int v, int* redi) {
 // ------------------------------------------------------------------------------------------
 // per-instance context (pointers into shared memory, scratch and the pools)
 // ------------------------------------------------------------------------------------------
+struct GridCtl;
+
 struct Ctx {
   int n, m, p, l, nsoc, nr, nUnits;
   const InstanceDesc* D;
@@ -126,6 +131,7 @@ struct Ctx {
   double* red;
   int* redi;
   double* sc;      // scalar broadcast area
+  GridCtl* grid;   // whole-GPU launch: the root jobs run on every CTA (null: this CTA alone)
 };
 
 // scalar slots in Ctx::sc
@@ -141,7 +147,7 @@ __device__ __forceinline__ long long* timers(Ctx& c) { return reinterpret_cast<l
 // ------------------------------------------------------------------------------------------
 // instance prologue: scaled copies of the data (equilibration.cpp:102-127)
 // ------------------------------------------------------------------------------------------
-__device__ __noinline__ void loadInstance(Ctx& c, const LaunchArgs& a) {
+static __device__ __noinline__ void loadInstance(Ctx& c, const LaunchArgs& a) {
   const InstanceDesc& D = *c.D;
   const double* dvec = a.dpool + D.dD;
   const double* evec = a.dpool + D.dE;
@@ -177,7 +183,7 @@ __device__ __noinline__ void loadInstance(Ctx& c, const LaunchArgs& a) {
 // ------------------------------------------------------------------------------------------
 // cone-set operations over all units of the instance (cone_set.cpp)
 // ------------------------------------------------------------------------------------------
-__device__ __noinline__ void coneUpdateScaling(Ctx& c, const double* s, const double* z) {
+static __device__ __noinline__ void coneUpdateScaling(Ctx& c, const double* s, const double* z) {
   FOR_T(t, c.l + c.nsoc) {
     if (t < c.l) {
       const int r = c.p + t;
@@ -192,7 +198,7 @@ __device__ __noinline__ void coneUpdateScaling(Ctx& c, const double* s, const do
 }
 
 // out = f(W) x on every cone row (Zero rows: 0, or eps * x for kHsEps).
-__device__ __noinline__ void coneApply(Ctx& c, int f, double eps, const double* x, double* out) {
+static __device__ __noinline__ void coneApply(Ctx& c, int f, double eps, const double* x, double* out) {
   FOR_T(r, c.p) out[r] = (f == kHsEps) ? eps * x[r] : 0.0;
   FOR_T(t, c.l + c.nsoc) {
     if (t < c.l) {
@@ -208,7 +214,7 @@ __device__ __noinline__ void coneApply(Ctx& c, int f, double eps, const double* 
 }
 
 // out = G x on the cone rows with the G eigenvalues prepared at factorisation (Zero rows: 0).
-__device__ __noinline__ void coneApplyG(Ctx& c, const double* x, double* out) {
+static __device__ __noinline__ void coneApplyG(Ctx& c, const double* x, double* out) {
   FOR_T(r, c.p) out[r] = 0.0;
   FOR_T(t, c.l + c.nsoc) {
     if (t < c.l) {
@@ -224,7 +230,7 @@ __device__ __noinline__ void coneApplyG(Ctx& c, const double* x, double* out) {
 }
 
 // Jordan product / inverse product (Zero rows -> 0).
-__device__ __noinline__ void coneProduct(Ctx& c, bool inverse, const double* u, const double* v, double* out) {
+static __device__ __noinline__ void coneProduct(Ctx& c, bool inverse, const double* u, const double* v, double* out) {
   FOR_T(r, c.p) out[r] = 0.0;
   FOR_T(t, c.l + c.nsoc) {
     if (t < c.l) {
@@ -241,7 +247,7 @@ __device__ __noinline__ void coneProduct(Ctx& c, bool inverse, const double* u, 
 }
 
 // ConeSet::maxStep (cone_set.cpp:108-115) as a block-wide min of per-unit limits.
-__device__ __noinline__ double coneMaxStep(Ctx& c, const double* x, const double* dx, double amax) {
+static __device__ __noinline__ double coneMaxStep(Ctx& c, const double* x, const double* dx, double amax) {
   double al = amax;
   FOR_T(t, c.l + c.nsoc) {
     if (t < c.l) {
@@ -257,7 +263,7 @@ __device__ __noinline__ double coneMaxStep(Ctx& c, const double* x, const double
 }
 
 // ConeSet::margins (cone_set.cpp:77-90): the NN block contributes ONE margin (its minimum).
-__device__ __noinline__ void coneMargins(Ctx& c, const double* x, double& mn, double& pos) {
+static __device__ __noinline__ void coneMargins(Ctx& c, const double* x, double& mn, double& pos) {
   double nnmin = INFINITY;
   FOR_T(t, c.l) nnmin = fmin(nnmin, x[c.p + t]);
   double smin = INFINITY, spos = 0.0;
@@ -275,14 +281,14 @@ __device__ __noinline__ void coneMargins(Ctx& c, const double* x, double& mn, do
   if (!isfinite(mn)) mn = 0.0;
 }
 
-__device__ void coneShift(Ctx& c, double* x, double alpha) {
+static __device__ void coneShift(Ctx& c, double* x, double alpha) {
   FOR_T(t, c.l) x[c.p + t] += alpha;
   FOR_T(b, c.nsoc) x[c.socOff[b]] += alpha;
   __syncthreads();
 }
 
 // shiftToInteriorCold (solver_impl.cpp:104-116 in the reference numbering of SolverImpl)
-__device__ void shiftToInteriorCold(Ctx& c, double* v, int degree) {
+static __device__ void shiftToInteriorCold(Ctx& c, double* v, int degree) {
   double mn, pos;
   coneMargins(c, v, mn, pos);
   const double deg = (double)max(degree, 1);
@@ -295,7 +301,7 @@ __device__ void shiftToInteriorCold(Ctx& c, double* v, int degree) {
   }
 }
 
-__device__ void ensureStrictlyInteriorWarm(Ctx& c, double* v) {
+static __device__ void ensureStrictlyInteriorWarm(Ctx& c, double* v) {
   double mn, pos;
   coneMargins(c, v, mn, pos);
   if (mn <= 1e-8) coneShift(c, v, -mn + 1e-6);
@@ -305,14 +311,14 @@ __device__ void ensureStrictlyInteriorWarm(Ctx& c, double* v) {
 // SpMVs with the scaled data (FP64)
 // ------------------------------------------------------------------------------------------
 // y = P_sym x (full symmetric CSR, one thread per row)
-__device__ __noinline__ void pmul(Ctx& c, const double* x, double* y) {
+static __device__ __noinline__ void pmul(Ctx& c, const double* x, double* y) {
   FOR_T(i, c.n) y[i] = csrDot(c.Pv, c.psCol, c.psRow[i], c.psRow[i + 1], x);
   __syncthreads();
 }
 
 // res = rhs - K sol for the statically-regularised K (the matrix refinement targets,
 // kkt_system.cpp:296-311): top = (P + epsP I) x + A'z, bottom = A x - (Hs + epsA I) z.
-__device__ __noinline__ double kktResidualImpl(Ctx& c, const DevSettings& st, const double* rhs, const double* sol,
+static __device__ __noinline__ double kktResidualImpl(Ctx& c, const DevSettings& st, const double* rhs, const double* sol,
                                   double* res, double& rhsNorm) {
   const int n = c.n, m = c.m;
   const double* xs = sol;
@@ -344,7 +350,7 @@ __device__ __noinline__ double kktResidualImpl(Ctx& c, const DevSettings& st, co
   return sqrt(acc2[0]) / rhsNorm;
 }
 
-__device__ double kktResidual(Ctx& c, const DevSettings& st, const double* rhs, const double* sol, double* res,
+static __device__ double kktResidual(Ctx& c, const DevSettings& st, const double* rhs, const double* sol, double* res,
                               double& rhsNorm) {
   const long long t0 = (st.record_timings && threadIdx.x == 0) ? clock64() : 0;
   const double r = kktResidualImpl(c, st, rhs, sol, res, rhsNorm);
@@ -932,6 +938,313 @@ __device__ void denseSolve(Ctx& c, const T* M, T* y) {
 }
 
 // ------------------------------------------------------------------------------------------
+// whole-GPU root (single large instance)
+// ------------------------------------------------------------------------------------------
+// One instance whose root is too large for one SM runs as a cooperative launch with one CTA
+// per SM: CTA 0 runs the interior-point iteration exactly as the batched kernel does, and at the
+// two root-sized steps, assembly + LDL' and the triangular solves, it posts a job that every
+// CTA runs with it. Jobs are the same tile operations in the same order per tile as the
+// single-CTA root, spread over the warps of the grid, with a grid barrier between dependent
+// steps (two per tile column of the factor, one per tile of each triangular pass).
+enum { kGridOpFactor = 1, kGridOpSolve = 2, kGridOpExit = 3 };
+
+struct GridCtl {
+  unsigned arrive;   // barrier: arrivals in the current round
+  unsigned gen;      // barrier: completed rounds
+  int error;         // a barrier wait ran out; every later barrier fails at once
+  int op;            // job posted by CTA 0
+  int arith;         // root arithmetic of the job: 0 FP64, 1 FP32, 2 double-float
+  int pad;
+  void* M;           // root of the job
+  void* y;           // solve vector (root arithmetic), rootTiles(nr) * 32 entries
+  double ep, ea;     // regularisation bumps of the assembly
+  Ctx ctx;           // CTA 0's instance context (pointers into global memory only)
+};
+
+template <typename T> struct ArithOf;
+template <> struct ArithOf<double> { static constexpr int v = 0; };
+template <> struct ArithOf<float> { static constexpr int v = 1; };
+template <> struct ArithOf<df64> { static constexpr int v = 2; };
+
+__device__ __forceinline__ unsigned long long globalNs() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Longest wait at one grid barrier. CTA 0's own work between two root jobs (cone scaling,
+// residuals, KKT residual products) takes milliseconds; a wait this long means a CTA is gone.
+constexpr unsigned long long kGridWaitNs = 30ull * 1000ull * 1000ull * 1000ull;
+
+// Grid-wide barrier of a cooperative launch (every CTA resident). Thread 0 of each CTA arrives
+// after a fence (release); the last arrival resets the count and opens the next round; the
+// others poll the round number and fence after it changes (acquire). Each wait is bounded by
+// kGridWaitNs: a wait that runs out records an error, and from then on every barrier of every
+// CTA returns false at once, so the launch always ends.
+static __device__ __noinline__ bool gridSync(GridCtl* g) {
+  __shared__ int sOk;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    volatile GridCtl* vg = g;
+    int ok = vg->error == 0;
+    if (ok) {
+      const unsigned gen = vg->gen;
+      __threadfence();
+      const unsigned prev = atomicAdd(&g->arrive, 1u);
+      if (prev == gridDim.x - 1) {
+        atomicExch(&g->arrive, 0u);
+        __threadfence();
+        atomicAdd(&g->gen, 1u);
+      } else {
+        const unsigned long long t0 = globalNs();
+        unsigned backoff = 32;  // ns, doubled up to 512 while the wait lasts
+        while (vg->gen == gen) {
+          if (vg->error) { ok = 0; break; }
+          if (globalNs() - t0 > kGridWaitNs) {
+            atomicExch(&g->error, 1);
+            ok = 0;
+            break;
+          }
+          __nanosleep(backoff);
+          if (backoff < 512) backoff <<= 1;
+        }
+      }
+      __threadfence();
+    }
+    sOk = ok;
+  }
+  __syncthreads();
+  return sOk != 0;
+}
+
+// Root assembly spread over the grid, the same writes as the single-CTA assembly in
+// assembleFactor: zero, then the distinct entries (padding identity, P diagonal + bump,
+// strictly-upper P, Zero-row A, Zero-row diagonal), then the cone-unit contributions (one target
+// root entry per thread, so no two threads add into the same entry).
+template <typename T>
+__device__ bool gridAssemble(GridCtl* g, const Ctx& c, const DevSettings& st, T* M, double ep, double ea) {
+  const InstanceDesc& D = *c.D;
+  const int n = c.n, nr = c.nr;
+  const int64_t gt = (int64_t)blockIdx.x * blockDim.x + threadIdx.x, gs = (int64_t)gridDim.x * blockDim.x;
+  const int64_t rs = rootSize(nr);
+  for (int64_t t = gt; t < rs; t += gs) M[t] = (T)0;
+  if (!gridSync(g)) return false;
+  for (int64_t i = nr + gt; i < (int64_t)rootTiles(nr) * kTile; i += gs) M[rootIdx(nr, (int)i, (int)i)] = (T)1;
+  for (int64_t i = gt; i < n; i += gs) {
+    const int src = c.pdiag[i];
+    M[rootIdx(nr, (int)i, (int)i)] = (T)(((src >= 0) ? c.Pu[src] : 0.0) + st.static_reg_P + ep);
+  }
+  for (int64_t k = gt; k < D.nPlow; k += gs) M[c.plowIdx[k]] = (T)c.Pu[c.plowSrc[k]];
+  for (int64_t k = gt; k < D.nAZ; k += gs) M[c.azIdx[k]] = (T)c.Av[c.azSrc[k]];
+  for (int64_t r = gt; r < c.p; r += gs) M[rootIdx(nr, n + (int)r, n + (int)r)] = (T)(-(st.static_reg_A + ea));
+  if (!gridSync(g)) return false;
+  for (int64_t t = gt; t < D.nTgt; t += gs) {
+    double acc = 0.0;
+    for (int q = c.tgtBeg[t]; q < c.tgtBeg[t + 1]; ++q) {
+      const int oi = c.contrib[3 * q], oj = c.contrib[3 * q + 1], d = c.contrib[3 * q + 2];
+      for (int r = 0; r < d; ++r) acc += c.Ad[oi + r] * c.T[oj + r];
+    }
+    M[c.tgtIdx[t]] += (T)acc;
+  }
+  return gridSync(g);
+}
+
+// Tiled right-looking LDL' of the root over every warp of the grid. Per tile column J: the
+// off-diagonal tiles of column J (one warp each), barrier, then the trailing update pairs
+// (I, K), J < K <= I, one warp each; warp 0 of CTA 0 takes the pair (J+1, J+1) and factors that
+// diagonal tile in the same step (one-column lookahead). Every tile receives its updates in
+// increasing J, as in the single-CTA factor, so both give the same bits. Only warp 0 of CTA 0
+// factors diagonal tiles, so the pivot statistics stay in CTA 0's shared memory (ps).
+template <typename T>
+__device__ bool gridLdlt(GridCtl* g, int nr, int nx, const DevSettings& st, T* M, PivotStats* ps) {
+  const int Tn = rootTiles(nr);
+  const int warp = threadIdx.x >> 5, W = blockDim.x >> 5;
+  const int gw = (int)blockIdx.x * W + warp, GW = (int)gridDim.x * W;
+  const bool lead = gw == 0;
+  if (lead) tileFactorDiag<T>(M, 0, nr, nx, st, ps);
+  if (!gridSync(g)) return false;
+  for (int J = 0; J + 1 < Tn; ++J) {
+    T* Ajj = M + tileBase(Tn, J, J);
+    for (int I = J + 1 + gw; I < Tn; I += GW) tileOffDiag<T>(M + tileBase(Tn, I, J), Ajj);
+    if (!gridSync(g)) return false;
+    const int rem = Tn - J - 1;
+    const long long npairs = (long long)rem * (rem + 1) / 2;
+    if (lead) {
+      T* An = M + tileBase(Tn, J + 1, J + 1);
+      const T* Ln = M + tileBase(Tn, J + 1, J);
+      tileSyrk<T>(An, Ln, Ln, Ajj);
+      tileFactorDiag<T>(An, J + 1, nr, nx, st, ps);
+    } else {
+      // pairs t >= 1 in row order: t = r (r + 1) / 2 + k, I = J + 1 + r, K = J + 1 + k, k <= r
+      for (long long t = gw; t < npairs; t += GW - 1) {
+        int r = (int)((sqrtf(8.0f * (float)t + 1.0f) - 1.0f) * 0.5f);
+        while ((long long)r * (r + 1) / 2 > t) --r;
+        while ((long long)(r + 1) * (r + 2) / 2 <= t) ++r;
+        const int k = (int)(t - (long long)r * (r + 1) / 2);
+        const int I = J + 1 + r, K = J + 1 + k;
+        tileSyrk<T>(M + tileBase(Tn, I, K), M + tileBase(Tn, I, J), M + tileBase(Tn, K, J), Ajj);
+      }
+    }
+    if (!gridSync(g)) return false;
+  }
+  return true;
+}
+
+// y_J <- Linv_JJ y_J (unit-lower inverse kept transposed in the diagonal tile), by one CTA:
+// 32 rows, each a dot product split over 4 lanes.
+template <typename T>
+__device__ void ctaDiagForward(const T* Ajj, T* yJ) {
+  constexpr int sd = 4, w = 32 / sd;
+  T tot = (T)0;
+  int i = 0, p = 0;
+  if ((int)threadIdx.x < 32 * sd) {
+    i = threadIdx.x / sd;
+    p = threadIdx.x % sd;
+    T acc = (T)0;
+    for (int col = p * w; col < (p + 1) * w && col < i; ++col) acc = accT(acc, Ajj[i * kTileLd + col], yJ[col]);
+    tot = groupSum(accEnd(acc), sd);
+  }
+  __syncthreads();
+  if ((int)threadIdx.x < 32 * sd && p == 0) yJ[i] = yJ[i] + tot;
+  __syncthreads();
+}
+
+// x_J <- Linv_JJ^T y_J, by one CTA.
+template <typename T>
+__device__ void ctaDiagBackward(const T* Ajj, T* yJ) {
+  constexpr int sd = 4, w = 32 / sd;
+  T tot = (T)0;
+  int i = 0, p = 0;
+  if ((int)threadIdx.x < 32 * sd) {
+    i = threadIdx.x / sd;
+    p = threadIdx.x % sd;
+    T acc = (T)0;
+    for (int row = p * w; row < (p + 1) * w; ++row)
+      if (row > i) acc = accT(acc, Ajj[row * kTileLd + i], yJ[row]);
+    tot = groupSum(accEnd(acc), sd);
+  }
+  __syncthreads();
+  if ((int)threadIdx.x < 32 * sd && p == 0) yJ[i] = yJ[i] + tot;
+  __syncthreads();
+}
+
+// y_I -= L_IJ y_J for one off-diagonal tile, one warp (lane = row of the tile).
+template <typename T>
+__device__ __forceinline__ void warpRowsForward(const T* Lij, const T* yJ, T* yI) {
+  const int lane = threadIdx.x & 31;
+  const T yv = yJ[lane];
+  T acc = (T)0;
+#pragma unroll 8
+  for (int col = 0; col < 32; ++col) acc = accT(acc, Lij[col * kTileLd + lane], shflT(yv, col));
+  yI[lane] = yI[lane] - accEnd(acc);
+}
+
+// y_K -= L_JK^T x_J for one off-diagonal tile, one warp (lane = column of the tile).
+template <typename T>
+__device__ __forceinline__ void warpRowsBackward(const T* Ljk, const T* xJ, T* yK) {
+  const int lane = threadIdx.x & 31;
+  const T xv = xJ[lane];
+  T acc = (T)0;
+#pragma unroll 8
+  for (int r2 = 0; r2 < 32; ++r2) acc = accT(acc, Ljk[lane * kTileLd + r2], shflT(xv, r2));
+  yK[lane] = yK[lane] - accEnd(acc);
+}
+
+// y <- M^-1 y over the grid. Forward step J: CTA 0 updates tile J+1 from tile J and solves its
+// diagonal block (lookahead), scales the finished tile J-1 by D, while the warps of the other
+// CTAs update tiles J+2 ... from tile J; one barrier per step. The backward pass mirrors it.
+// Needs at least two CTAs.
+template <typename T>
+__device__ bool gridSolve(GridCtl* g, int nr, const T* M, T* y) {
+  const int Tn = rootTiles(nr);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, W = blockDim.x >> 5;
+  const bool drv = blockIdx.x == 0;
+  const int ww = ((int)blockIdx.x - 1) * W + warp, WW = ((int)gridDim.x - 1) * W;
+  auto scaleTile = [&](int J) {
+    T* yJ = y + J * 32;
+    yJ[lane] /= M[tileBase(Tn, J, J) + lane * kTileLd + lane];
+  };
+  if (drv) ctaDiagForward<T>(M, y);
+  if (!gridSync(g)) return false;
+  for (int J = 0; J + 1 < Tn; ++J) {
+    const T* yJ = y + J * 32;
+    if (drv) {
+      if (warp == 0) warpRowsForward<T>(M + tileBase(Tn, J + 1, J), yJ, y + (J + 1) * 32);
+      else if (warp == 1 && J >= 1) scaleTile(J - 1);
+      __syncthreads();
+      ctaDiagForward<T>(M + tileBase(Tn, J + 1, J + 1), y + (J + 1) * 32);
+    } else {
+      for (int I = J + 2 + ww; I < Tn; I += WW) warpRowsForward<T>(M + tileBase(Tn, I, J), yJ, y + I * 32);
+    }
+    if (!gridSync(g)) return false;
+  }
+  if (drv) {
+    // tiles Tn-2 and Tn-1 are not scaled yet (the forward steps scale tiles up to Tn-3)
+    if (warp < 2 && Tn - 1 - warp >= 0) scaleTile(Tn - 1 - warp);
+    __syncthreads();
+    ctaDiagBackward<T>(M + tileBase(Tn, Tn - 1, Tn - 1), y + (Tn - 1) * 32);
+  }
+  if (!gridSync(g)) return false;
+  for (int J = Tn - 1; J >= 1; --J) {
+    const T* xJ = y + J * 32;
+    if (drv) {
+      if (warp == 0) warpRowsBackward<T>(M + tileBase(Tn, J, J - 1), xJ, y + (J - 1) * 32);
+      __syncthreads();
+      ctaDiagBackward<T>(M + tileBase(Tn, J - 1, J - 1), y + (J - 1) * 32);
+    } else {
+      for (int K = J - 2 - ww; K >= 0; K -= WW) warpRowsBackward<T>(M + tileBase(Tn, J, K), xJ, y + K * 32);
+    }
+    if (!gridSync(g)) return false;
+  }
+  return true;
+}
+
+// One posted job, run by every CTA (CTA 0 passes its pivot statistics).
+template <typename T>
+__device__ bool gridJobT(GridCtl* g, const DevSettings& st, int op, PivotStats* ps) {
+  volatile GridCtl* vg = g;
+  T* M = reinterpret_cast<T*>(vg->M);
+  const Ctx& c = g->ctx;
+  if (op == kGridOpFactor)
+    return gridAssemble<T>(g, c, st, M, vg->ep, vg->ea) && gridLdlt<T>(g, c.nr, c.n, st, M, ps);
+  if (op == kGridOpSolve) return gridSolve<T>(g, c.nr, M, reinterpret_cast<T*>(vg->y));
+  return false;
+}
+
+// CTAs 1 .. of a whole-GPU launch: wait for a job, run it, until CTA 0 posts the exit.
+template <typename FT>
+__device__ void gridWorker(GridCtl* g, const DevSettings& st) {
+  for (;;) {
+    if (!gridSync(g)) return;
+    volatile GridCtl* vg = g;
+    const int op = vg->op, arith = vg->arith;
+    if (op == kGridOpExit) return;
+    bool ok;
+    if constexpr (sizeof(FT) == 4)
+      ok = (arith == 1) ? gridJobT<float>(g, st, op, nullptr) : gridJobT<df64>(g, st, op, nullptr);
+    else
+      ok = gridJobT<double>(g, st, op, nullptr);
+    if (!ok) return;
+  }
+}
+
+// CTA 0: post a job (the barrier publishes it) and run it with the other CTAs.
+template <typename T>
+__device__ bool gridPost(Ctx& c, const DevSettings& st, int op, T* M, T* y, double ep, double ea, PivotStats* ps) {
+  GridCtl* g = c.grid;
+  if (threadIdx.x == 0) {
+    g->op = op;
+    g->arith = ArithOf<T>::v;
+    g->M = M;
+    g->y = y;
+    g->ep = ep;
+    g->ea = ea;
+  }
+  if (!gridSync(g)) return false;
+  return gridJobT<T>(g, st, op, ps);
+}
+
+// ------------------------------------------------------------------------------------------
 // reduced KKT: assembly + factorisation, and one solve through it
 // ------------------------------------------------------------------------------------------
 // Builds the root for the current cone scaling with extra diagonal bumps (ep on x rows, -ea on
@@ -958,6 +1271,30 @@ __device__ __noinline__ void assembleFactor(Ctx& c, const DevSettings& st, T* M,
       socPrepareG(c.sp[b], epsA);
       for (int k = a0; k < a1; k += d) socApplyG(c.sp[b], c.cu + off, d, c.Ad + k, c.T + k);
     }
+  }
+  if (c.grid) {
+    // whole-GPU launch: the assembly and the LDL' run on every CTA
+    PivotStats* ps = reinterpret_cast<PivotStats*>(c.sc + SC_COUNT);
+    if (threadIdx.x == 0) {
+      ps->nreg = 0;
+      ps->zero = 0;
+      ps->wrong = 0;
+      ps->minAbs = INFINITY;
+    }
+    __syncthreads();
+    const long long t1 = (st.record_timings && threadIdx.x == 0) ? clock64() : 0;
+    const bool ok = gridPost<T>(c, st, kGridOpFactor, M, (T*)nullptr, ep, ea, ps);
+    __syncthreads();
+    const bool regularized = st.linear_solver == 2;
+    fail = !ok ? 1 : (regularized ? (((double)ps->nreg > 0.05 * (double)nr) ? 1 : 0) : ps->zero);
+    wrongSign = ps->wrong;
+    minAbsD = ok ? ps->minAbs : NAN;
+    __syncthreads();
+    if (st.record_timings && threadIdx.x == 0) {
+      timers(c)[TM_ASSEMBLE] += t1 - t0;
+      timers(c)[TM_LDLT] += clock64() - t1;
+    }
+    return;
   }
   const int64_t rs = rootSize(nr);
   for (int64_t t = threadIdx.x; t < rs; t += blockDim.x) M[t] = (T)0;
@@ -1012,7 +1349,15 @@ __device__ __noinline__ void reducedSolve(Ctx& c, const DevSettings& st, const T
   for (int i = nr + (int)threadIdx.x; i < rootTiles(nr) * kTile; i += blockDim.x) y[i] = (T)0;
   __syncthreads();
   const long long t0 = (st.record_timings && threadIdx.x == 0) ? clock64() : 0;
-  denseSolve<T>(c, M, y);
+  if (c.grid) {
+    // whole-GPU launch; a failed barrier leaves a non-finite solution, which the caller's
+    // finiteness test turns into NumericalError
+    if (!gridPost<T>(c, st, kGridOpSolve, const_cast<T*>(M), y, 0.0, 0.0, nullptr) && threadIdx.x == 0)
+      y[0] = (T)NAN;
+    __syncthreads();
+  } else {
+    denseSolve<T>(c, M, y);
+  }
   if (st.record_timings && threadIdx.x == 0) timers(c)[TM_DSOLVE] += clock64() - t0;
   FOR_T(j, n) sol[j] = (double)y[j];
   FOR_T(r, p) sol[n + r] = (double)y[n + r];
@@ -1098,7 +1443,7 @@ __device__ void solveOnce(Ctx& c, const DevSettings& st, const FactState& fs, co
     reducedSolve<FT>(c, st, rootT<FT>(c), fs.ea, rhs, sol);
 }
 
-__device__ __noinline__ bool vecFinite(Ctx& c, const double* v, int len) {
+static __device__ __noinline__ bool vecFinite(Ctx& c, const double* v, int len) {
   int bad = 0;
   FOR_T(i, len) bad |= !finiteBits(v[i]);
   return blockOrInt(bad, c.redi) == 0;
@@ -1538,7 +1883,7 @@ __device__ __noinline__ void solveInstance(Ctx& c, const LaunchArgs& a, int inst
     R.fp64_fallbacks = (int)c.sc[SC_NFB];
     R.refine_steps = (int)c.sc[SC_RSTEPS];
     R.factor_attempts = (int)c.sc[SC_ATTEMPTS];
-    R.error_code = 0;
+    R.error_code = (c.grid && reinterpret_cast<volatile GridCtl*>(c.grid)->error) ? 1 : 0;
     const long long tot = clock64() - tStart;
     R.cycles[0] = tot;
     if (st.record_timings) {
@@ -1563,7 +1908,7 @@ __device__ __noinline__ void solveInstance(Ctx& c, const LaunchArgs& a, int inst
 // kernel: persistent CTAs over an atomic instance queue
 // ------------------------------------------------------------------------------------------
 // Points the per-instance context at shared memory, the CTA's scratch and the pools (thread 0).
-__device__ void setupCtx(Ctx& c, const LaunchArgs& a, int inst, unsigned char* smem, double* scratch, int* sRedi) {
+static __device__ void setupCtx(Ctx& c, const LaunchArgs& a, int inst, unsigned char* smem, double* scratch, int* sRedi) {
   const SmemLayout& L = a.lay;
   const InstanceDesc& D = a.desc[inst];
   c.D = &D;
@@ -1604,6 +1949,7 @@ __device__ void setupCtx(Ctx& c, const LaunchArgs& a, int inst, unsigned char* s
   c.red = reinterpret_cast<double*>(smem + L.redOff);
   c.sc = c.red + 128;
   c.redi = sRedi;
+  c.grid = nullptr;
 }
 
 // ------------------------------------------------------------------------------------------
@@ -1612,12 +1958,38 @@ __device__ void setupCtx(Ctx& c, const LaunchArgs& a, int inst, unsigned char* s
 // kMaxThreads / kMinBlocks: the large-root form (up to 256 threads, registers for one CTA per
 // SM) and the small-root form (up to 64 threads, at least 8 CTAs per SM: small instances are
 // bound by FP64 latency, so more of them resident per SM is more throughput).
+//
+// Whole-GPU form (a.grid set; large-root form only): one large instance, a cooperative launch
+// with one CTA per SM. CTA 0 runs the iteration, the other CTAs run the root jobs it posts (see
+// gridSync); the vectors, the root and the solve vector are in CTA 0's scratch (global memory)
+// so every CTA can reach them.
 template <typename FT, int kMaxThreads, int kMinBlocks>
 __global__ void __launch_bounds__(kMaxThreads, kMinBlocks) ipmKernel(LaunchArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ int sInst;
   __shared__ int sRedi[4];
   __shared__ Ctx c;
+  if constexpr (kMaxThreads >= 256) {
+    if (a.grid) {
+      GridCtl* g = a.grid;
+      if (blockIdx.x == 0) {
+        const int inst = a.order[0];
+        if (threadIdx.x == 0) {
+          setupCtx(c, a, inst, smem, a.scratch, sRedi);
+          c.grid = g;
+          g->ctx = c;
+        }
+        __syncthreads();
+        loadInstance(c, a);
+        solveInstance<FT>(c, a, inst);
+        if (threadIdx.x == 0) g->op = kGridOpExit;
+        gridSync(g);
+      } else {
+        gridWorker<FT>(g, a.st);
+      }
+      return;
+    }
+  }
   double* scratch = a.scratch + (int64_t)blockIdx.x * a.scratchStride;
   for (;;) {
     if (threadIdx.x == 0) sInst = atomicAdd(a.counter, 1);
@@ -1640,7 +2012,7 @@ __global__ void __launch_bounds__(kMaxThreads, kMinBlocks) ipmKernel(LaunchArgs 
 // all in the equilibrated space and mapped back through D, E, c (P^ = c D P D, q^ = c D q,
 // A^ = E A D, b^ = E b, x = D x^).
 // ------------------------------------------------------------------------------------------
-__device__ __noinline__ void adjointInstance(Ctx& c, const LaunchArgs& a) {
+static __device__ __noinline__ void adjointInstance(Ctx& c, const LaunchArgs& a) {
   const InstanceDesc& D = *c.D;
   const double* Bs = a.bwd + D.bwdOff;
   const BwdLayout bl = bwdLayout(c.nr, c.n, c.m, c.nsoc);
@@ -1693,132 +2065,49 @@ __device__ __noinline__ void adjointInstance(Ctx& c, const LaunchArgs& a) {
   __syncthreads();
 }
 
-__global__ void __launch_bounds__(256) adjointKernel(LaunchArgs a) {
-  extern __shared__ __align__(16) unsigned char smem[];
-  __shared__ int sInst;
-  __shared__ int sRedi[4];
-  __shared__ Ctx c;
-  double* scratch = a.scratch + (int64_t)blockIdx.x * a.scratchStride;
-  for (;;) {
-    if (threadIdx.x == 0) sInst = atomicAdd(a.counter, 1);
-    __syncthreads();
-    const int slot = sInst;
-    __syncthreads();
-    if (slot >= a.count) break;
-    const int inst = a.order[slot];
-    if (threadIdx.x == 0) setupCtx(c, a, inst, smem, scratch, sRedi);
-    __syncthreads();
-    loadInstance(c, a);
-    adjointInstance(c, a);
-  }
-}
 
-cudaError_t launchAdjoint(const LaunchArgs& a, int grid, int block, size_t smem, cudaStream_t stream) {
-  cudaError_t e = cudaFuncSetAttribute(adjointKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e != cudaSuccess) return e;
-  adjointKernel<<<grid, block, smem, stream>>>(a);
-  return cudaGetLastError();
-}
-
-// explicit instantiations through the host launchers: the small-root form for blocks of up to
-// 64 threads, the large-root form otherwise
-using IpmFn = void (*)(LaunchArgs);
-static IpmFn ipmFor(bool fp32, int block) {
-  if (block <= 64) return fp32 ? ipmKernel<float, 64, 8> : ipmKernel<double, 64, 8>;
-  return fp32 ? ipmKernel<float, 256, 1> : ipmKernel<double, 256, 1>;
-}
-
-cudaError_t launchIpm(const LaunchArgs& a, int grid, int block, size_t smem, bool fp32, cudaStream_t stream) {
-  const IpmFn k = ipmFor(fp32, block);
+// Host launchers of the kernels above, per root arithmetic FT (float: mixed precision, double:
+// FP64) and launch form; explicitly instantiated in cxg_ipm_f32.cu, cxg_ipm_f32s.cu and
+// cxg_ipm_f64.cu.
+template <typename FT, int kMaxThreads, int kMinBlocks>
+cudaError_t launchIpmFormT(const LaunchArgs& a, int grid, int block, size_t smem, cudaStream_t stream) {
+  void (*k)(LaunchArgs) = ipmKernel<FT, kMaxThreads, kMinBlocks>;
   cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   k<<<grid, block, smem, stream>>>(a);
   return cudaGetLastError();
 }
 
-cudaError_t ipmOccupancy(int* blocksPerSM, int block, size_t smem, bool fp32) {
-  const IpmFn k = ipmFor(fp32, block);
+template <typename FT, int kMaxThreads, int kMinBlocks>
+cudaError_t ipmOccupancyFormT(int* blocksPerSM, int block, size_t smem) {
+  void (*k)(LaunchArgs) = ipmKernel<FT, kMaxThreads, kMinBlocks>;
   cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocksPerSM, k, block, smem);
 }
 
-}  // namespace cxg
-
-// ------------------------------------------------------------------------------------------
-// diagnostic: the dense root LDL' and solve of the IPM kernel on one given matrix (one CTA)
-// ------------------------------------------------------------------------------------------
-namespace cxg {
-
-template <typename T>
-__global__ void __launch_bounds__(256) denseProbeKernel(int nr, int nx, const double* K, const double* b,
-                                                         DevSettings st, double* Lout, double* Dout, double* xout,
-                                                         long long* cyc, int* flags) {
-  extern __shared__ __align__(16) unsigned char smem[];
-  __shared__ Ctx c;
-  __shared__ double scArea[160];
-  T* M = reinterpret_cast<T*>(smem);
-  const int Tn = rootTiles(nr);
-  const int64_t rs = rootSize(nr);
-  T* y = M + rs;
-  if (threadIdx.x == 0) {
-    c.nr = nr;
-    c.n = nx;
-    c.red = scArea;
-    c.sc = scArea + 128;
-  }
-  for (int64_t t = threadIdx.x; t < rs; t += blockDim.x) M[t] = (T)0;
-  __syncthreads();
-  for (int i = nr + (int)threadIdx.x; i < Tn * kTile; i += blockDim.x) M[rootIdx(nr, i, i)] = (T)1;
-  for (int t = threadIdx.x; t < nr * nr; t += blockDim.x) {
-    const int i = t % nr, j = t / nr;
-    if (i >= j) M[rootIdx(nr, i, j)] = (T)K[t];
-  }
-  __syncthreads();
-  int fail = 0, wrong = 0;
-  double mind = 0.0;
-  const long long t0 = clock64();
-  denseLdlt<T>(c, M, st, fail, wrong, mind);
-  const long long t1 = clock64();
-  for (int t = threadIdx.x; t < nr * nr; t += blockDim.x) {
-    const int i = t % nr, j = t / nr;
-    Lout[t] = (i > j) ? (double)M[rootIdx(nr, i, j)] : ((i == j) ? 1.0 : 0.0);
-  }
-  for (int i = threadIdx.x; i < nr; i += blockDim.x) Dout[i] = (double)M[rootIdx(nr, i, i)];
-  for (int i = threadIdx.x; i < Tn * kTile; i += blockDim.x) y[i] = (i < nr) ? (T)b[i] : (T)0;
-  __syncthreads();
-  const long long t2 = clock64();
-  denseSolve<T>(c, M, y);
-  const long long t3 = clock64();
-  for (int i = threadIdx.x; i < nr; i += blockDim.x) xout[i] = (double)y[i];
-  if (threadIdx.x == 0) {
-    cyc[0] = t1 - t0;
-    cyc[1] = t3 - t2;
-    flags[0] = fail;
-    flags[1] = wrong;
-  }
-}
-
-template <typename T>
-static cudaError_t probeLaunch(int nr, int nx, const double* K, const double* b, const DevSettings& st, int threads,
-                               double* L, double* D, double* x, long long* cyc, int* flags) {
-  const size_t smem = (size_t)(rootSize(nr) + (int64_t)rootTiles(nr) * kTile) * sizeof(T);
-  cudaError_t e = cudaFuncSetAttribute(denseProbeKernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+template <typename FT>
+cudaError_t launchIpmGridT(const LaunchArgs& a, GridCtl* g, int grid, size_t smem, cudaStream_t stream) {
+  void (*k)(LaunchArgs) = ipmKernel<FT, 256, 1>;
+  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  denseProbeKernel<T><<<1, threads, smem>>>(nr, nx, K, b, st, L, D, x, cyc, flags);
-  return cudaGetLastError();
+  LaunchArgs av = a;
+  av.grid = g;
+  void* args[] = {(void*)&av};
+  return cudaLaunchCooperativeKernel((const void*)k, dim3(grid), dim3(256), args, smem, stream);
 }
 
-size_t denseProbeSmem(int arith, int nr) {
-  const size_t elem = (arith == 1) ? 4 : 8;
-  return (size_t)(rootSize(nr) + (int64_t)rootTiles(nr) * kTile) * elem;
+template <typename FT>
+cudaError_t ipmGridOccupancyT(int* blocksPerSM, size_t smem) {
+  return ipmOccupancyFormT<FT, 256, 1>(blocksPerSM, 256, smem);
 }
 
-cudaError_t launchDenseProbe(int arith, int nr, int nx, const double* K, const double* b, const DevSettings& st,
-                             int threads, double* L, double* D, double* x, long long* cyc, int* flags) {
-  if (arith == 1) return probeLaunch<float>(nr, nx, K, b, st, threads, L, D, x, cyc, flags);
-  if (arith == 2) return probeLaunch<df64>(nr, nx, K, b, st, threads, L, D, x, cyc, flags);
-  return probeLaunch<double>(nr, nx, K, b, st, threads, L, D, x, cyc, flags);
-}
+// Explicit instantiation (EXT empty) or declaration (EXT extern) of the launchers of one form.
+#define CXG_IPM_FORM(EXT, FT, TH, MB)                                                            \
+  EXT template cudaError_t launchIpmFormT<FT, TH, MB>(const LaunchArgs&, int, int, size_t, cudaStream_t); \
+  EXT template cudaError_t ipmOccupancyFormT<FT, TH, MB>(int*, int, size_t);
+#define CXG_IPM_GRID(EXT, FT)                                                                    \
+  EXT template cudaError_t launchIpmGridT<FT>(const LaunchArgs&, GridCtl*, int, size_t, cudaStream_t); \
+  EXT template cudaError_t ipmGridOccupancyT<FT>(int*, size_t);
 
 }  // namespace cxg

@@ -8,6 +8,8 @@
 
 namespace cxg {
 
+struct GridCtl;
+
 // Dynamic shared-memory layout of one launch (byte offsets), sized for the largest instance of
 // the launch. Vectors go to shared memory when they fit, else to the CTA's scratch.
 struct SmemLayout {
@@ -55,9 +57,15 @@ struct LaunchArgs {
   int64_t scratchStride;
   DevSettings st;
   SmemLayout lay;
+  struct GridCtl* grid;   // whole-GPU form of one instance (cooperative launch), else null
 };
 
 cudaError_t launchIpm(const LaunchArgs& a, int grid, int block, size_t smem, bool fp32, cudaStream_t stream);
+// Whole-GPU form for a single instance (args.count == 1): a cooperative launch of `grid` CTAs of
+// 256 threads; `ctl` is a zeroed device control block of gridCtlBytes().
+size_t gridCtlBytes();
+cudaError_t launchIpmGrid(const LaunchArgs& a, GridCtl* ctl, int grid, size_t smem, bool fp32, cudaStream_t stream);
+cudaError_t ipmGridOccupancy(int* blocksPerSM, size_t smem, bool fp32);
 // One adjoint solve per instance with the saved final factorisation (same launch shape as the
 // forward groups).
 cudaError_t launchAdjoint(const LaunchArgs& a, int grid, int block, size_t smem, cudaStream_t stream);

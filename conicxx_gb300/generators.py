@@ -140,3 +140,111 @@ def config3_batch(count=1024, base_seed=0):
 def x_target(seed, n):
     """x_target ~ N(0,1) for the differentiable-layer loss L = 1/2 ||x* - x_target||^2."""
     return _rng(7, seed).standard_normal(n)
+
+
+def _distinct_per_row(rng, count, upper, k):
+    """(count, k) integers in [0, upper), distinct within each row."""
+    idx = rng.integers(0, upper, size=(count, k))
+    while True:
+        srt = np.sort(idx, axis=1)
+        dup = (np.diff(srt, axis=1) == 0).any(axis=1)
+        if not dup.any():
+            return idx
+        idx[dup] = rng.integers(0, upper, size=(int(dup.sum()), k))
+
+
+def _upper_of_gram(F, extra_diag):
+    """Upper triangle (CSC) of F'F + extra_diag I for a scipy sparse F (structural pattern)."""
+    import scipy.sparse as sp
+
+    G = (F.T @ F + extra_diag * sp.identity(F.shape[1], format="csc")).tocoo()
+    keep = G.row <= G.col
+    return Csc.from_coo(F.shape[1], F.shape[1], G.row[keep], G.col[keep], G.data[keep])
+
+
+def large_sparse_qp(seed, n=20000, m_zero=2000, m_nonneg=24000, n_soc=2000, soc_dim=2, m_col_nnz=3, a_row_nnz=8,
+                    p_reg=1e-3):
+    """One large sparse conic QP (the mixed-precision single-instance workload).
+
+    P = M'M + p_reg I with M n x n holding m_col_nnz N(0,1) entries per column at distinct random
+    rows (upper triangle stored); A m x n with a_row_nnz N(0,1) entries per row at distinct random
+    columns; cones Zero^m_zero x R^m_nonneg_+ x n_soc Q^soc_dim. Feasible and bounded by the
+    primal-dual pair construction of random_conic_qp (x0 ~ N(0,1), interior s0/z0,
+    b = A x0 + s0, q = -P x0 - A' z0). Defaults: n = 20000, m = 30000."""
+    import scipy.sparse as sp
+
+    rng = _rng(2, seed)
+    soc = [soc_dim] * n_soc
+    m = m_zero + m_nonneg + soc_dim * n_soc
+    mr = _distinct_per_row(rng, n, n, m_col_nnz)
+    M = sp.csc_matrix((rng.standard_normal(n * m_col_nnz), (mr.ravel(), np.repeat(np.arange(n), m_col_nnz))),
+                      shape=(n, n))
+    P = _upper_of_gram(M, p_reg)
+    ac = _distinct_per_row(rng, m, n, a_row_nnz)
+    A = Csc.from_coo(m, n, np.repeat(np.arange(m), a_row_nnz), ac.ravel(), rng.standard_normal(m * a_row_nnz))
+    x0 = rng.standard_normal(n)
+    s0 = _interior(rng, m_zero, m_nonneg, soc, free_zero=False)
+    z0 = _interior(rng, m_zero, m_nonneg, soc, free_zero=True)
+    b = A.matvec(x0) + s0
+    q = -sym_upper_matvec(P, x0) - A.rmatvec(z0)
+    qp = QP(P=P, q=q, A=A, b=b, zero=m_zero, nonneg=m_nonneg, soc=soc, name=f"large_sparse_qp[{seed}]")
+    qp.validate()
+    return qp
+
+
+def group_lasso_socp(seed, groups=4000, group_size=16, rows_per_group=20, row_nnz=12, blocks=64, coupling=0.05,
+                     active=0.10, lam=0.1):
+    """Group-sparse robust least squares as an SOCP (the block-sparse large-instance workload).
+
+    minimise 1/2 ||F x - g||^2 + lam sum_j t_j  s.t.  ||x_Gj||_2 <= t_j, for `groups` groups of
+    `group_size` variables. F is (groups*rows_per_group) x (groups*group_size) with row_nnz N(0,1)
+    entries per row: `blocks` diagonal blocks, a fraction `coupling` of each row's entries at
+    random columns outside its block. g = F x_true + 0.01 N(0,1), x_true nonzero (N(0,1)) on a
+    fraction `active` of the groups. Standard form in the variables (x, t), n = groups *
+    (group_size + 1): P = F'F (upper, on x), q = (-F'g, lam 1), one SOC block (t_j, x_Gj) of
+    dimension group_size + 1 per group (rows -e, b = 0); the constant 1/2 ||g||^2 is dropped.
+    Defaults: 4000 groups of 16, F 80000 x 64000, n = 68000."""
+    import scipy.sparse as sp
+
+    rng = _rng(4, seed)
+    nx = groups * group_size
+    rows = groups * rows_per_group
+    blocks = max(1, min(blocks, groups))
+    rb = -(-rows // blocks)
+    cb = -(-nx // blocks)
+    blk = np.minimum(np.arange(rows) // rb, blocks - 1)
+    lo = blk * cb
+    hi = np.minimum(lo + cb, nx)
+    # within-block columns (distinct per row), a fraction replaced by random coupling columns
+    width = hi - lo
+    u = rng.random((rows, row_nnz))
+    cols = lo[:, None] + np.floor(u * width[:, None]).astype(np.int64)
+    far = rng.random((rows, row_nnz)) < coupling
+    cols[far] = rng.integers(0, nx, size=int(far.sum()))
+    F = sp.coo_matrix((rng.standard_normal(rows * row_nnz), (np.repeat(np.arange(rows), row_nnz), cols.ravel())),
+                      shape=(rows, nx)).tocsc()
+    F.sum_duplicates()
+    x_true = np.zeros(nx)
+    on = rng.random(groups) < active
+    for j in np.where(on)[0]:
+        x_true[j * group_size:(j + 1) * group_size] = rng.standard_normal(group_size)
+    g = F @ x_true + 0.01 * rng.standard_normal(rows)
+    n = nx + groups
+    Px = _upper_of_gram(F, 0.0)
+    P = Csc((n, n), np.concatenate([Px.indptr, np.full(groups, Px.indptr[-1], np.int32)]).astype(np.int32),
+            Px.indices, Px.data)
+    q = np.concatenate([-(F.T @ g), np.full(groups, lam)])
+    d = group_size + 1
+    r, c = [], []
+    for j in range(groups):
+        r.append(j * d)
+        c.append(nx + j)
+        for k in range(group_size):
+            r.append(j * d + 1 + k)
+            c.append(j * group_size + k)
+    m = groups * d
+    A = Csc.from_coo(m, n, np.asarray(r), np.asarray(c), -np.ones(len(r)))
+    b = np.zeros(m)
+    qp = QP(P=P, q=q, A=A, b=b, zero=0, nonneg=0, soc=[d] * groups, name=f"group_lasso[{seed}]")
+    qp.validate()
+    return qp

@@ -94,7 +94,11 @@ typedef struct cxg_settings {
   int threads_per_instance;   /* 0 = by root size (32 up to 32 rows, 64 up to 64, 128 up to 128,
                                  else 256); else 32, 64, 128 or 256 */
   int differentiable;         /* keep each instance's final factorisation, scaling and iterate on the
-                                 device so backward() can reuse them (default 0; cxg_solver: 1) */
+                                 device so backward() can reuse them (default 0; cxg_solver: 1);
+                                 ignored for whole-GPU roots above 8192 rows */
+  int whole_gpu_root;         /* single-instance handles (count 1): 0 = automatic, the root is spread
+                                 over every SM when it has more than 512 rows (always beyond 4096);
+                                 1 = always; -1 = never (one CTA, roots up to 4096 rows) */
 } cxg_settings;
 
 /* conicxx::Info (include/conicxx/solution.h:18-26) plus Solution::objective/status and counters. */
@@ -266,7 +270,10 @@ int cxg_cones_eval(int op, int zero_dim, int nonneg_dim, int n_soc, const int* s
  * run by one CTA of `threads` (32..256, a multiple of 32) threads in arith 0 = FP64, 1 = FP32, 2 = double-float; then the
  * triangular solves for K x = b. Outputs (each may be NULL): L (nr x nr unit lower, column-major),
  * D (nr), x (nr), cycles[2] = SM clock cycles of {factorisation, solve}, flags[2] = {exact zero /
- * too many corrections, wrong-signed pivot}. Allocates its own device buffers. */
+ * too many corrections, wrong-signed pivot}. Allocates its own device buffers.
+ * threads = -1: the whole-GPU root of a single large instance instead (every SM, cooperative
+ * launch); cycles then hold nanoseconds and flags has a third entry, 1 if a grid barrier wait ran
+ * out. */
 int cxg_dense_ldlt(int nr, int nx, const double* K, const double* b, int arith, int threads, int linear_solver,
                    double* L, double* D, double* x, long long* cycles, int* flags);
 /* Host equilibration of the set-up path (Equilibration::compute, src/conicxx/kkt/equilibration.cpp:8-100):

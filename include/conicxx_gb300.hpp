@@ -179,6 +179,7 @@ struct Settings {
   Scalar mixed_fallback_tol = 1e-10;
   int threads_per_instance = 0;
   bool differentiable = true;  // keep the final factorisation for backward()
+  int whole_gpu_root = 0;      // 0 automatic (roots above 512 rows use every SM), 1 always, -1 never
 };
 
 // Status / Info / Solution (include/conicxx/solution.h:9-39).
@@ -283,6 +284,7 @@ inline cxg_settings toC(const Settings& s) {
   c.mixed_fallback_tol = s.mixed_fallback_tol;
   c.threads_per_instance = s.threads_per_instance;
   c.differentiable = s.differentiable ? 1 : 0;
+  c.whole_gpu_root = s.whole_gpu_root;
   return c;
 }
 }  // namespace detail

@@ -363,17 +363,19 @@ def test_autotune_keeps_results():
         assert np.max(np.abs(a - b)) <= 1e-5 * max(1.0, np.max(np.abs(b))), i
 
 
+@pytest.mark.parametrize("whole_gpu_root", [-1, 1])
 @pytest.mark.parametrize("precision", [_abi.PRECISION_FP64, _abi.PRECISION_MIXED])
-def test_larger_instance_root_in_scratch(oracle_mod, precision):
+def test_larger_instance_root_in_scratch(oracle_mod, precision, whole_gpu_root):
     """One instance with a 550-row root (n = 500, m = 600: Zero^50 x R^400_+ x 50 Q^3): the root
     and its factor live in the CTA's scratch rather than shared memory, and the triangular solve
-    takes its block-parallel form (more than six tiles). Same status as the oracle, iterations
-    within +-1, x within 1e-6 relative."""
+    takes its block-parallel form (more than six tiles); with whole_gpu_root = 1 the root is
+    spread over every SM instead. Same status as the oracle, iterations within +-1, x within 1e-6
+    relative."""
     from conicxx_gb300 import Solver
 
     qp = generators.random_conic_qp(3, n=500, m_zero=50, m_nonneg=400, soc=(3,) * 50, density=0.02)
     S = Solver()
-    assert S.setup(qp, precision=precision, warm_start=0)
+    assert S.setup(qp, precision=precision, warm_start=0, whole_gpu_root=whole_gpu_root)
     sol = S.solve()
     xo, _, _, io, _ = oracle_mod.solve(qp, warm_start=0)
     assert sol.status == io["status"] == 1
