@@ -211,6 +211,8 @@ static const int kCtaMaxRoot = 4096;
 static const int kGridAutoRoot = 512;
 static const int kGridMaxRoot = 131072;
 static const int kGridMaxAdjointRoot = 8192;
+// shared memory of the whole-GPU trailing update: 9 tiles of 32 x 33 8-byte entries
+static const int64_t kGridStageBytes = 9ll * kTileElems * 8;
 
 static int chooseBlock(int nrMax, int requested) {
   if (requested == 32 || requested == 64 || requested == 128 || requested == 256) return requested;
@@ -289,6 +291,10 @@ static int buildGroups(cxg_batch* B) {
     } else if (!gridMode && fp32 && used + root32Bytes <= budget) {
       L.rootInSmem = 1;
       used += root32Bytes;
+    }
+    if (gridMode) {
+      // tile staging area of the whole-GPU trailing update, where the root would otherwise go
+      used += kGridStageBytes;
     }
     L.total = used;
     g.smem = (size_t)used;

@@ -958,8 +958,14 @@ struct GridCtl {
   void* M;           // root of the job
   void* y;           // solve vector (root arithmetic), rootTiles(nr) * 32 entries
   double ep, ea;     // regularisation bumps of the assembly
+  int64_t stageOff;  // byte offset of the tile staging area in dynamic shared memory
   Ctx ctx;           // CTA 0's instance context (pointers into global memory only)
 };
+
+// Tile staging area of the whole-GPU trailing update: the diagonal tile and up to 4 + 4 panel
+// tiles of one 4x4-tile super-block.
+constexpr int kStageTiles = 9;
+constexpr int64_t gridStageBytes(int elemBytes) { return (int64_t)kStageTiles * kTileElems * elemBytes; }
 
 template <typename T> struct ArithOf;
 template <> struct ArithOf<double> { static constexpr int v = 0; };
@@ -1049,40 +1055,79 @@ __device__ bool gridAssemble(GridCtl* g, const Ctx& c, const DevSettings& st, T*
   return gridSync(g);
 }
 
-// Tiled right-looking LDL' of the root over every warp of the grid. Per tile column J: the
-// off-diagonal tiles of column J (one warp each), barrier, then the trailing update pairs
-// (I, K), J < K <= I, one warp each; warp 0 of CTA 0 takes the pair (J+1, J+1) and factors that
-// diagonal tile in the same step (one-column lookahead). Every tile receives its updates in
-// increasing J, as in the single-CTA factor, so both give the same bits. Only warp 0 of CTA 0
-// factors diagonal tiles, so the pivot statistics stay in CTA 0's shared memory (ps).
+// One 32x32 tile, global -> shared memory, 16-byte vectors (tiles start on 16-byte boundaries:
+// kTileElems * 4 bytes is a multiple of 16 and the root base is 16-byte aligned).
 template <typename T>
-__device__ bool gridLdlt(GridCtl* g, int nr, int nx, const DevSettings& st, T* M, PivotStats* ps) {
+__device__ __forceinline__ void stageTile(T* dst, const T* src) {
+  constexpr int n16 = (int)(kTileElems * sizeof(T) / 16);
+  static_assert(kTileElems * sizeof(T) % 16 == 0, "tile size");
+  const uint4* s = reinterpret_cast<const uint4*>(src);
+  uint4* d = reinterpret_cast<uint4*>(dst);
+  for (int i = threadIdx.x; i < n16; i += blockDim.x) d[i] = s[i];
+}
+
+// Tiled right-looking LDL' of the root over the whole grid. Per tile column J:
+//  (A) the off-diagonal tiles of column J, one warp each; barrier;
+//  (B) the trailing update C_IK -= L_IJ D_J L_KJ^T, J < K <= I, in super-blocks of 4x4 tiles, one
+//      CTA each: the diagonal tile and the super-block's panel tiles L_IJ, L_KJ are staged in
+//      shared memory once and the 8 warps take its (up to 16) C tiles, so each panel tile is read
+//      from L2 once per super-block instead of once per C tile. CTA 0 takes the first
+//      super-block, whose tile (J+1, J+1) its warp 0 updates and factors in the same step
+//      (one-column lookahead); barrier.
+// Every tile receives its updates in increasing J through the same tile routines as the
+// single-CTA factor, so both give the same bits. Only warp 0 of CTA 0 factors diagonal tiles, so
+// the pivot statistics stay in CTA 0's shared memory (ps). `stage` holds gridStageBytes.
+template <typename T>
+__device__ bool gridLdlt(GridCtl* g, int nr, int nx, const DevSettings& st, T* M, PivotStats* ps, T* stage) {
   const int Tn = rootTiles(nr);
   const int warp = threadIdx.x >> 5, W = blockDim.x >> 5;
   const int gw = (int)blockIdx.x * W + warp, GW = (int)gridDim.x * W;
-  const bool lead = gw == 0;
-  if (lead) tileFactorDiag<T>(M, 0, nr, nx, st, ps);
+  const bool cta0 = blockIdx.x == 0;
+  if (cta0 && warp == 0) tileFactorDiag<T>(M, 0, nr, nx, st, ps);
   if (!gridSync(g)) return false;
   for (int J = 0; J + 1 < Tn; ++J) {
     T* Ajj = M + tileBase(Tn, J, J);
     for (int I = J + 1 + gw; I < Tn; I += GW) tileOffDiag<T>(M + tileBase(Tn, I, J), Ajj);
     if (!gridSync(g)) return false;
     const int rem = Tn - J - 1;
-    const long long npairs = (long long)rem * (rem + 1) / 2;
-    if (lead) {
-      T* An = M + tileBase(Tn, J + 1, J + 1);
-      const T* Ln = M + tileBase(Tn, J + 1, J);
-      tileSyrk<T>(An, Ln, Ln, Ajj);
-      tileFactorDiag<T>(An, J + 1, nr, nx, st, ps);
-    } else {
-      // pairs t >= 1 in row order: t = r (r + 1) / 2 + k, I = J + 1 + r, K = J + 1 + k, k <= r
-      for (long long t = gw; t < npairs; t += GW - 1) {
-        int r = (int)((sqrtf(8.0f * (float)t + 1.0f) - 1.0f) * 0.5f);
-        while ((long long)r * (r + 1) / 2 > t) --r;
-        while ((long long)(r + 1) * (r + 2) / 2 <= t) ++r;
-        const int k = (int)(t - (long long)r * (r + 1) / 2);
-        const int I = J + 1 + r, K = J + 1 + k;
-        tileSyrk<T>(M + tileBase(Tn, I, K), M + tileBase(Tn, I, J), M + tileBase(Tn, K, J), Ajj);
+    const int nb = (rem + 3) >> 2;
+    const long long nsb = (long long)nb * (nb + 1) / 2;
+    // super-blocks in row order: sb = r (r + 1) / 2 + k, tile rows J+1+4r.., tile columns J+1+4k..
+    // CTA 0 takes sb = 0 only; CTAs 1.. take 1, 2, ... cyclically
+    const long long step = cta0 ? nsb : (long long)gridDim.x - 1;
+    for (long long sb = cta0 ? 0 : (long long)blockIdx.x; sb < nsb; sb += step) {
+      int r = (int)((sqrtf(8.0f * (float)sb + 1.0f) - 1.0f) * 0.5f);
+      while ((long long)r * (r + 1) / 2 > sb) --r;
+      while ((long long)(r + 1) * (r + 2) / 2 <= sb) ++r;
+      const int k = (int)(sb - (long long)r * (r + 1) / 2);
+      const int I0 = J + 1 + 4 * r, K0 = J + 1 + 4 * k;
+      const int ni = min(4, Tn - I0), nk = min(4, Tn - K0);
+      const bool diagSb = r == k;
+      __syncthreads();  // the previous super-block's tiles are done with the staging area
+      stageTile<T>(stage, Ajj);
+      for (int t = 0; t < ni; ++t) stageTile<T>(stage + (1 + t) * kTileElems, M + tileBase(Tn, I0 + t, J));
+      if (!diagSb)
+        for (int t = 0; t < nk; ++t) stageTile<T>(stage + (5 + t) * kTileElems, M + tileBase(Tn, K0 + t, J));
+      __syncthreads();
+      const T* Ds = stage;
+      const T* As = stage + kTileElems;
+      const T* Bs = diagSb ? As : stage + 5 * kTileElems;
+      const int ntiles = ni * nk;
+      int t0 = warp, tstep = W;
+      if (cta0) {
+        // tile 0 of super-block 0 is (J+1, J+1): warp 0 updates and factors it
+        if (warp == 0) {
+          T* An = M + tileBase(Tn, J + 1, J + 1);
+          tileSyrk<T>(An, As, As, Ds);
+          tileFactorDiag<T>(An, J + 1, nr, nx, st, ps);
+          t0 = ntiles;
+        }
+        tstep = W - 1;
+      }
+      for (int t = t0; t < ntiles; t += tstep) {
+        const int a = t / nk, b = t % nk;
+        if (diagSb && b > a) continue;
+        tileSyrk<T>(M + tileBase(Tn, I0 + a, K0 + b), As + a * kTileElems, Bs + b * kTileElems, Ds);
       }
     }
     if (!gridSync(g)) return false;
@@ -1205,8 +1250,10 @@ __device__ bool gridJobT(GridCtl* g, const DevSettings& st, int op, PivotStats* 
   volatile GridCtl* vg = g;
   T* M = reinterpret_cast<T*>(vg->M);
   const Ctx& c = g->ctx;
+  extern __shared__ __align__(16) unsigned char dynSmem[];
+  T* stage = reinterpret_cast<T*>(dynSmem + vg->stageOff);
   if (op == kGridOpFactor)
-    return gridAssemble<T>(g, c, st, M, vg->ep, vg->ea) && gridLdlt<T>(g, c.nr, c.n, st, M, ps);
+    return gridAssemble<T>(g, c, st, M, vg->ep, vg->ea) && gridLdlt<T>(g, c.nr, c.n, st, M, ps, stage);
   if (op == kGridOpSolve) return gridSolve<T>(g, c.nr, M, reinterpret_cast<T*>(vg->y));
   return false;
 }
@@ -1978,6 +2025,7 @@ __global__ void __launch_bounds__(kMaxThreads, kMinBlocks) ipmKernel(LaunchArgs 
           setupCtx(c, a, inst, smem, a.scratch, sRedi);
           c.grid = g;
           g->ctx = c;
+          g->stageOff = a.lay.rootOff;  // the root itself is in scratch in this form
         }
         __syncthreads();
         loadInstance(c, a);

@@ -74,6 +74,8 @@ __global__ void __launch_bounds__(256, 1) denseProbeGridKernel(int nr, int nx, c
                                                                double* Dout, double* xout, long long* cyc,
                                                                int* flags) {
   __shared__ PivotStats sPs;
+  extern __shared__ __align__(16) unsigned char stageSmem[];
+  T* stage = reinterpret_cast<T*>(stageSmem);
   const int Tn = rootTiles(nr);
   const int64_t rs = rootSize(nr);
   const int64_t gt = (int64_t)blockIdx.x * blockDim.x + threadIdx.x, gs = (int64_t)gridDim.x * blockDim.x;
@@ -94,7 +96,7 @@ __global__ void __launch_bounds__(256, 1) denseProbeGridKernel(int nr, int nx, c
   for (int64_t i = gt; i < (int64_t)Tn * kTile; i += gs) y[i] = (i < nr) ? (T)b[i] : (T)0;
   ok = ok && gridSync(g);
   const unsigned long long t0 = globalNs();
-  ok = ok && gridLdlt<T>(g, nr, nx, st, M, &sPs);
+  ok = ok && gridLdlt<T>(g, nr, nx, st, M, &sPs, stage);
   const unsigned long long t1 = globalNs();
   for (int64_t t = gt; t < nn; t += gs) {
     const int i = (int)(t % nr), j = (int)(t / nr);
@@ -121,7 +123,10 @@ static cudaError_t probeGridLaunch(int nr, int nx, const double* K, const double
   int dev = 0, numSM = 0, occ = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&numSM, cudaDevAttrMultiProcessorCount, dev);
-  if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, denseProbeGridKernel<T>, 256, 0);
+  const size_t smem = (size_t)gridStageBytes((int)sizeof(T));
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(denseProbeGridKernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, denseProbeGridKernel<T>, 256, smem);
   if (e != cudaSuccess) return e;
   if (occ * numSM < 2) return cudaErrorInvalidConfiguration;
   T *M = nullptr, *y = nullptr;
@@ -135,7 +140,7 @@ static cudaError_t probeGridLaunch(int nr, int nx, const double* K, const double
     DevSettings stv = st;
     void* args[] = {&nrv, &nxv, (void*)&K, (void*)&b, &stv, (void*)&M, (void*)&y, (void*)&g,
                     (void*)&L, (void*)&D, (void*)&x, (void*)&cyc, (void*)&flags};
-    e = cudaLaunchCooperativeKernel((const void*)denseProbeGridKernel<T>, dim3(occ * numSM), dim3(256), args, 0,
+    e = cudaLaunchCooperativeKernel((const void*)denseProbeGridKernel<T>, dim3(occ * numSM), dim3(256), args, smem,
                                     nullptr);
     if (e == cudaSuccess) e = cudaDeviceSynchronize();
   }
