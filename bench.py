@@ -317,6 +317,7 @@ def run_gb300(args, rank, world, local_rank):
                   "cpu_1core_ms": float(np.median(c_ms)), "iterations_gpu_mixed": int(sol0m.info["iterations"]),
                   "iterations_gpu": int(sol0.info["iterations"]), "iterations_cpu": int(oi0["iterations"]),
                   "status_gpu": int(sol0.status), "status_cpu": int(oi0["status"])}
+        large = large_instance_leg(orc)
         ncpu = os.cpu_count() or 1
         sample = qps[:args.cpu_sample]
         cpu_wall, cpu_st, _ = orc.batch_solve(sample, ncpu, warm_start=0)
@@ -350,11 +351,77 @@ def run_gb300(args, rank, world, local_rank):
                               "bound by FP64 pipe and barrier latency of the slowest instances, not by HBM"},
             fwd_bwd=fwd_bwd,
             single_instance=single,
+            large_instance=large,
             setup_s=setup_s,
         )
     if tune_report is not None:
         result["autotune"] = tune_report.strip().splitlines()
     return ms, wall, clocks, launches_per_step, solved_frac, statuses, result
+
+
+def large_instance_leg(orc):
+    """Single large instances on the whole GPU (root spread over every SM), mixed precision:
+    - the n=20000, m=30000 sparse QP (root of 22000 rows): its first 3 iterations, timed (the full
+      solve runs to MaxIterations at 200 iterations, as the oracle does on this family at
+      n=2000), with the FP32 factor's throughput;
+    - the group-lasso SOCP with 1000 groups of 16 (n=17000, 1000 SOC blocks of dimension 17),
+      solved to completion;
+    - the sparse QP family at n=1000 (root of 1100 rows) against the oracle on one host core."""
+    from conicxx_gb300 import Solver, generators
+
+    out = {}
+    qp = generators.large_sparse_qp(0)
+    S = Solver()
+    assert S.setup(qp, precision=1, warm_start=0, record_timings=1, max_iter=3)
+    t0 = time.perf_counter()
+    sol = S.solve()
+    dt = time.perf_counter() - t0
+    inf = sol.info
+    nr = qp.n + qp.zero
+    per_fact = inf["time_ldlt_s"] / max(1, inf["factor_attempts"])
+    clock_hz = 2.07e9
+    fp32_peak = 152 * 128 * clock_hz / 1e12  # FP32 FMA/s of the CUDA cores at the maximum SM clock
+    tfma = (nr ** 3 / 6) / per_fact / 1e12
+    out["sparse_qp_n20000"] = {
+        "workload": "n=20000, m=30000, Zero^2000 x R^24000_+ x 2000 Q^2, P=M'M+1e-3 I (3 nnz/col), A 8 nnz/row",
+        "root_rows": nr, "iterations_timed": int(inf["iterations"]), "s_per_iteration": dt / max(1, inf["iterations"]),
+        "factorisations": int(inf["factor_attempts"]), "fp32_assembly_ldlt_s": per_fact,
+        "fp32_ldlt_tfma_s": tfma, "fp32_cuda_core_peak_tfma_s": fp32_peak, "frac": tfma / fp32_peak,
+        "dense_solve_s": inf["time_dense_solve_s"], "fp64_fallbacks": int(inf["fp64_fallbacks"])}
+    qpg = generators.group_lasso_socp(0, groups=1000)
+    S = Solver()
+    assert S.setup(qpg, precision=1, warm_start=0, record_timings=1)
+    t0 = time.perf_counter()
+    sol = S.solve()
+    dt = time.perf_counter() - t0
+    inf = sol.info
+    st_, fe_, sz_ = qpg.kkt_residuals(sol.x, sol.s, sol.z)
+    out["group_lasso_g1000"] = {
+        "workload": "1000 groups of 16: n=17000, F 20000 x 16000 (12 nnz/row, 64 blocks + 5% coupling), 1000 Q^17",
+        "solve_s": dt, "status": int(sol.status), "iterations": int(inf["iterations"]),
+        "fp64_fallbacks": int(inf["fp64_fallbacks"]), "ldlt_s": inf["time_ldlt_s"],
+        "dense_solve_s": inf["time_dense_solve_s"], "kkt_residuals": [float(st_), float(fe_), float(sz_)]}
+    qps = generators.large_sparse_qp(0, n=1000, m_zero=100, m_nonneg=1200, n_soc=100)
+    times = {}
+    for prec in (0, 1):
+        S = Solver()
+        assert S.setup(qps, precision=prec, warm_start=0)
+        S.solve()
+        t0 = time.perf_counter()
+        sol = S.solve()
+        times[prec] = (time.perf_counter() - t0, sol)
+    O = orc.OracleSolver()
+    assert O.setup(qps, warm_start=0)
+    t0 = time.perf_counter()
+    xo, _, _, io = O.solve()
+    tc = time.perf_counter() - t0
+    out["sparse_qp_n1000"] = {
+        "workload": "n=1000, m=1500, Zero^100 x R^1200_+ x 100 Q^2 (same family), root of 1100 rows",
+        "gpu_fp64_s": times[0][0], "gpu_mixed_s": times[1][0], "cpu_1core_s": tc,
+        "status_gpu": int(times[1][1].status), "status_cpu": int(io["status"]),
+        "iterations_gpu": int(times[1][1].info["iterations"]), "iterations_cpu": int(io["iterations"]),
+        "x_maxdiff_rel": float(np.max(np.abs(times[1][1].x - xo)) / max(1.0, np.max(np.abs(xo))))}
+    return out
 
 
 def run_reference(args, rank, world):

@@ -205,14 +205,14 @@ static int64_t r2(int64_t v) { return (v + 1) & ~int64_t(1); }
 // Group boundaries on the root dimension nr; each group gets a shared-memory layout sized for
 // its largest instance.
 static const int kBucketEdges[] = {32, 64, 96, 128, 160, 192, 256, 384, 512, 1024, 2048, 4096};
-// Root sizes: largest one-CTA root; a single instance above kGridAutoRoot rows takes the
-// whole-GPU root (whole_gpu_root = 0), which accepts up to kGridMaxRoot rows (a 70 GB FP64 root).
+// Root sizes: the largest one-CTA root; cxg_solver spreads roots above kGridAutoRoot rows over
+// every SM (whole_gpu_root = 0), which accepts up to kGridMaxRoot rows (a 70 GB FP64 root).
 static const int kCtaMaxRoot = 4096;
 static const int kGridAutoRoot = 512;
 static const int kGridMaxRoot = 131072;
 static const int kGridMaxAdjointRoot = 8192;
-// shared memory of the whole-GPU trailing update: 9 tiles of 32 x 33 8-byte entries
-static const int64_t kGridStageBytes = 9ll * kTileElems * 8;
+// shared memory of the whole-GPU trailing update (8-byte entries; see gridStageBytes)
+static const int64_t kGridStageBytes = (2ll * kTile * 128 + 16ll * kTileElems) * 8;
 
 static int chooseBlock(int nrMax, int requested) {
   if (requested == 32 || requested == 64 || requested == 128 || requested == 256) return requested;
@@ -438,10 +438,10 @@ extern "C" int cxg_batch_create(cxg_batch** out, int count, const cxg_problem* p
                         " exceeds the one-CTA root (4096 rows); a single instance (count 1, whole_gpu_root >= 0) "
                         "takes the whole-GPU root up to 131072 rows");
   }
-  // One instance with a root beyond what one SM factors quickly: spread the root over every SM.
+  // One instance whose root one CTA cannot hold, or when asked: spread the root over every SM.
+  // (cxg_solver_setup asks for it from kGridAutoRoot rows on.)
   const int nr0 = problems[0].n + problems[0].zero_dim;
-  const bool gridMode = count == 1 && (st.whole_gpu_root == 1 || (st.whole_gpu_root == 0 && nr0 > kGridAutoRoot) ||
-                                       nr0 > kCtaMaxRoot);
+  const bool gridMode = count == 1 && (st.whole_gpu_root == 1 || nr0 > kCtaMaxRoot);
   // the adjoint keeps an FP64 copy of the final factor and solves with it on one CTA: offered up
   // to 8192 root rows
   if (gridMode && nr0 > kGridMaxAdjointRoot) st.differentiable = 0;
@@ -928,7 +928,11 @@ extern "C" int cxg_solver_setup(cxg_solver* S, const cxg_problem* pr, const cxg_
     st.differentiable = 1;
   }
   S->st = st;
-  int rc = cxg_batch_create(&S->batch, 1, pr, &st);
+  // automatic whole-GPU root for a single instance: one SM factors roots up to a few hundred rows
+  // in well under a millisecond, larger ones are faster spread over every SM
+  cxg_settings bst = st;
+  if (bst.whole_gpu_root == 0 && pr->n + pr->zero_dim > kGridAutoRoot) bst.whole_gpu_root = 1;
+  int rc = cxg_batch_create(&S->batch, 1, pr, &bst);
   if (rc) return rc;
   S->n = pr->n;
   S->m = pr->m;

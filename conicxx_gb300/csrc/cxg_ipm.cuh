@@ -962,10 +962,12 @@ struct GridCtl {
   Ctx ctx;           // CTA 0's instance context (pointers into global memory only)
 };
 
-// Tile staging area of the whole-GPU trailing update: the diagonal tile and up to 4 + 4 panel
-// tiles of one 4x4-tile super-block.
-constexpr int kStageTiles = 9;
-constexpr int64_t gridStageBytes(int elemBytes) { return (int64_t)kStageTiles * kTileElems * elemBytes; }
+// Shared memory of the whole-GPU trailing update for one 128x128 super-block (4x4 tiles): the
+// panel rows A[32][128] and the D-scaled panel columns B[32][128] (k-major), and the 16 result
+// tiles in tile layout.
+constexpr int kSbDim = 128;
+constexpr int kStageElems = 2 * kTile * kSbDim + 16 * kTileElems;
+constexpr int64_t gridStageBytes(int elemBytes) { return (int64_t)kStageElems * elemBytes; }
 
 template <typename T> struct ArithOf;
 template <> struct ArithOf<double> { static constexpr int v = 0; };
@@ -1028,7 +1030,7 @@ static __device__ __noinline__ bool gridSync(GridCtl* g) {
 // strictly-upper P, Zero-row A, Zero-row diagonal), then the cone-unit contributions (one target
 // root entry per thread, so no two threads add into the same entry).
 template <typename T>
-__device__ bool gridAssemble(GridCtl* g, const Ctx& c, const DevSettings& st, T* M, double ep, double ea) {
+__device__ __noinline__ bool gridAssemble(GridCtl* g, const Ctx& c, const DevSettings& st, T* M, double ep, double ea) {
   const InstanceDesc& D = *c.D;
   const int n = c.n, nr = c.nr;
   const int64_t gt = (int64_t)blockIdx.x * blockDim.x + threadIdx.x, gs = (int64_t)gridDim.x * blockDim.x;
@@ -1055,30 +1057,135 @@ __device__ bool gridAssemble(GridCtl* g, const Ctx& c, const DevSettings& st, T*
   return gridSync(g);
 }
 
-// One 32x32 tile, global -> shared memory, 16-byte vectors (tiles start on 16-byte boundaries:
-// kTileElems * 4 bytes is a multiple of 16 and the root base is 16-byte aligned).
+// Four consecutive entries of a shared-memory row (16-byte aligned for 4-byte T, two 16-byte
+// halves for 8-byte T).
 template <typename T>
-__device__ __forceinline__ void stageTile(T* dst, const T* src) {
-  constexpr int n16 = (int)(kTileElems * sizeof(T) / 16);
-  static_assert(kTileElems * sizeof(T) % 16 == 0, "tile size");
-  const uint4* s = reinterpret_cast<const uint4*>(src);
-  uint4* d = reinterpret_cast<uint4*>(dst);
-  for (int i = threadIdx.x; i < n16; i += blockDim.x) d[i] = s[i];
+__device__ __forceinline__ void lds4(const T* p, T (&v)[4]) {
+  if constexpr (sizeof(T) == 4) {
+    const float4 f = *reinterpret_cast<const float4*>(p);
+    v[0] = f.x; v[1] = f.y; v[2] = f.z; v[3] = f.w;
+  } else {
+#pragma unroll
+    for (int i = 0; i < 4; ++i) v[i] = p[i];
+  }
+}
+
+// C -= A D B^T for one super-block of up to 4x4 tiles, by one CTA of 256 threads:
+// rows I0 .. I0+ni-1 and columns K0 .. K0+nk-1 (tile indices); only tiles with column <= row when
+// the super-block is on the diagonal. A = the panel tiles L_IJ, B = L_KJ, D = diag of tile (J, J).
+// The panel is staged k-major in shared memory (B pre-scaled by D exactly as tileSyrk scales
+// it), each thread accumulates an 8x8 block of the 128x128 product over k = 0..31 in the order
+// tileSyrk uses (so every entry gets the same bits), the results go to shared memory in tile
+// layout, and the C tiles are updated with 16-byte vector loads and stores.
+template <typename T>
+__device__ __noinline__ void superSyrk(T* M, int Tn, int J, int I0, int K0, int ni, int nk, bool diagSb, T* sm) {
+  T* As = sm;
+  T* Bs = sm + kTile * kSbDim;
+  T* Cs = sm + 2 * kTile * kSbDim;
+  const T* Ajj = M + tileBase(Tn, J, J);
+  const int tid = threadIdx.x;
+  {
+    // thread tid stages column i = tid & 127 of the panel for k = tid >> 7, +2, ... (all loads of
+    // the thread issued before any store, so their latencies overlap)
+    const int i = tid & (kSbDim - 1), a = i >> 5, rr = i & 31, k0 = tid >> 7;
+    const T* pa = (a < ni) ? M + tileBase(Tn, I0 + a, J) + rr : nullptr;
+    const T* pb = (a < nk) ? M + tileBase(Tn, K0 + a, J) + rr : nullptr;
+    constexpr int kPer = 8;  // 256 threads: two k rows per step, 8 steps per half
+#pragma unroll 1
+    for (int h = 0; h < 2; ++h) {
+      T va[kPer], vb[kPer], dk[kPer];
+#pragma unroll
+      for (int t = 0; t < kPer; ++t) {
+        const int k = k0 + 2 * (h * kPer + t);
+        va[t] = pa ? pa[k * kTileLd] : (T)0;
+        vb[t] = pb ? pb[k * kTileLd] : (T)0;
+        dk[t] = Ajj[k * kTileLd + k];
+      }
+#pragma unroll
+      for (int t = 0; t < kPer; ++t) {
+        const int k = k0 + 2 * (h * kPer + t);
+        As[k * kSbDim + i] = va[t];
+        Bs[k * kSbDim + i] = pb ? vb[t] * dk[t] : (T)0;
+      }
+    }
+  }
+  __syncthreads();
+  const int tx = tid & 15, ty = tid >> 4;  // rows tx*4 + {0..3, 64..67}, columns ty*4 + {0..3, 64..67}
+  T acc[8][8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i)
+#pragma unroll
+    for (int j = 0; j < 8; ++j) acc[i][j] = (T)0;
+#pragma unroll 2
+  for (int k = 0; k < kTile; ++k) {
+    T a0[4], a1[4], b0[4], b1[4];
+    lds4(As + k * kSbDim + tx * 4, a0);
+    lds4(As + k * kSbDim + 64 + tx * 4, a1);
+    lds4(Bs + k * kSbDim + ty * 4, b0);
+    lds4(Bs + k * kSbDim + 64 + ty * 4, b1);
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        acc[i][j] = accT(acc[i][j], a0[i], b0[j]);
+        acc[i][4 + j] = accT(acc[i][4 + j], a0[i], b1[j]);
+        acc[4 + i][j] = accT(acc[4 + i][j], a1[i], b0[j]);
+        acc[4 + i][4 + j] = accT(acc[4 + i][4 + j], a1[i], b1[j]);
+      }
+  }
+  // results to shared memory in tile layout (tile t = a * 4 + b), padding entries zeroed
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    const int R = (i < 4) ? tx * 4 + i : 64 + tx * 4 + (i - 4);
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const int Cc = (j < 4) ? ty * 4 + j : 64 + ty * 4 + (j - 4);
+      Cs[((R >> 5) * 4 + (Cc >> 5)) * kTileElems + (Cc & 31) * kTileLd + (R & 31)] = accEnd(acc[i][j]);
+    }
+  }
+  for (int idx = tid; idx < 16 * kTile; idx += blockDim.x) Cs[(idx >> 5) * kTileElems + (idx & 31) * kTileLd + 32] = (T)0;
+  __syncthreads();
+  // C -= result, 16-byte vectors; each thread loads a batch of its vectors before storing any
+  constexpr int per16 = 16 / (int)sizeof(T);
+  constexpr int vpt = kTileElems / per16;  // vectors per tile
+  constexpr int kBatch = 4;
+  const int total = 16 * vpt;
+  for (int base = 0; base < total; base += kBatch * (int)blockDim.x) {
+    uint4 cv[kBatch];
+    T* cp[kBatch];
+#pragma unroll
+    for (int u = 0; u < kBatch; ++u) {
+      const int v = base + u * (int)blockDim.x + tid;
+      const int t = v / vpt, a = t >> 2, b = t & 3;
+      const bool use = v < total && a < ni && b < nk && !(diagSb && b > a);
+      cp[u] = use ? M + tileBase(Tn, I0 + a, K0 + b) + (v - t * vpt) * per16 : nullptr;
+      if (use) cv[u] = *reinterpret_cast<const uint4*>(cp[u]);
+    }
+#pragma unroll
+    for (int u = 0; u < kBatch; ++u) {
+      if (!cp[u]) continue;
+      const int v = base + u * (int)blockDim.x + tid;
+      alignas(16) T c[per16];
+      alignas(16) T d[per16];
+      *reinterpret_cast<uint4*>(c) = cv[u];
+      *reinterpret_cast<uint4*>(d) = *reinterpret_cast<const uint4*>(Cs + v * per16);
+#pragma unroll
+      for (int e = 0; e < per16; ++e) c[e] = c[e] - d[e];
+      *reinterpret_cast<uint4*>(cp[u]) = *reinterpret_cast<const uint4*>(c);
+    }
+  }
 }
 
 // Tiled right-looking LDL' of the root over the whole grid. Per tile column J:
 //  (A) the off-diagonal tiles of column J, one warp each; barrier;
 //  (B) the trailing update C_IK -= L_IJ D_J L_KJ^T, J < K <= I, in super-blocks of 4x4 tiles, one
-//      CTA each: the diagonal tile and the super-block's panel tiles L_IJ, L_KJ are staged in
-//      shared memory once and the 8 warps take its (up to 16) C tiles, so each panel tile is read
-//      from L2 once per super-block instead of once per C tile. CTA 0 takes the first
-//      super-block, whose tile (J+1, J+1) its warp 0 updates and factors in the same step
-//      (one-column lookahead); barrier.
-// Every tile receives its updates in increasing J through the same tile routines as the
-// single-CTA factor, so both give the same bits. Only warp 0 of CTA 0 factors diagonal tiles, so
-// the pivot statistics stay in CTA 0's shared memory (ps). `stage` holds gridStageBytes.
+//      CTA each (superSyrk). CTA 0 takes the first super-block, then its warp 0 factors the tile
+//      (J+1, J+1) in the same step (one-column lookahead); barrier.
+// Every root entry receives its updates in increasing J with the same operations and rounding as
+// the single-CTA factor, so both give the same bits. Only warp 0 of CTA 0 factors diagonal tiles,
+// so the pivot statistics stay in CTA 0's shared memory (ps). `stage` holds gridStageBytes.
 template <typename T>
-__device__ bool gridLdlt(GridCtl* g, int nr, int nx, const DevSettings& st, T* M, PivotStats* ps, T* stage) {
+__device__ __noinline__ bool gridLdlt(GridCtl* g, int nr, int nx, const DevSettings& st, T* M, PivotStats* ps, T* stage) {
   const int Tn = rootTiles(nr);
   const int warp = threadIdx.x >> 5, W = blockDim.x >> 5;
   const int gw = (int)blockIdx.x * W + warp, GW = (int)gridDim.x * W;
@@ -1101,33 +1208,11 @@ __device__ bool gridLdlt(GridCtl* g, int nr, int nx, const DevSettings& st, T* M
       while ((long long)(r + 1) * (r + 2) / 2 <= sb) ++r;
       const int k = (int)(sb - (long long)r * (r + 1) / 2);
       const int I0 = J + 1 + 4 * r, K0 = J + 1 + 4 * k;
-      const int ni = min(4, Tn - I0), nk = min(4, Tn - K0);
-      const bool diagSb = r == k;
-      __syncthreads();  // the previous super-block's tiles are done with the staging area
-      stageTile<T>(stage, Ajj);
-      for (int t = 0; t < ni; ++t) stageTile<T>(stage + (1 + t) * kTileElems, M + tileBase(Tn, I0 + t, J));
-      if (!diagSb)
-        for (int t = 0; t < nk; ++t) stageTile<T>(stage + (5 + t) * kTileElems, M + tileBase(Tn, K0 + t, J));
-      __syncthreads();
-      const T* Ds = stage;
-      const T* As = stage + kTileElems;
-      const T* Bs = diagSb ? As : stage + 5 * kTileElems;
-      const int ntiles = ni * nk;
-      int t0 = warp, tstep = W;
+      __syncthreads();  // the previous super-block is done with the staging area
+      superSyrk<T>(M, Tn, J, I0, K0, min(4, Tn - I0), min(4, Tn - K0), r == k, stage);
       if (cta0) {
-        // tile 0 of super-block 0 is (J+1, J+1): warp 0 updates and factors it
-        if (warp == 0) {
-          T* An = M + tileBase(Tn, J + 1, J + 1);
-          tileSyrk<T>(An, As, As, Ds);
-          tileFactorDiag<T>(An, J + 1, nr, nx, st, ps);
-          t0 = ntiles;
-        }
-        tstep = W - 1;
-      }
-      for (int t = t0; t < ntiles; t += tstep) {
-        const int a = t / nk, b = t % nk;
-        if (diagSb && b > a) continue;
-        tileSyrk<T>(M + tileBase(Tn, I0 + a, K0 + b), As + a * kTileElems, Bs + b * kTileElems, Ds);
+        __syncthreads();
+        if (warp == 0) tileFactorDiag<T>(M + tileBase(Tn, J + 1, J + 1), J + 1, nr, nx, st, ps);
       }
     }
     if (!gridSync(g)) return false;
@@ -1200,7 +1285,7 @@ __device__ __forceinline__ void warpRowsBackward(const T* Ljk, const T* xJ, T* y
 // CTAs update tiles J+2 ... from tile J; one barrier per step. The backward pass mirrors it.
 // Needs at least two CTAs.
 template <typename T>
-__device__ bool gridSolve(GridCtl* g, int nr, const T* M, T* y) {
+__device__ __noinline__ bool gridSolve(GridCtl* g, int nr, const T* M, T* y) {
   const int Tn = rootTiles(nr);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, W = blockDim.x >> 5;
   const bool drv = blockIdx.x == 0;
@@ -1260,7 +1345,7 @@ __device__ bool gridJobT(GridCtl* g, const DevSettings& st, int op, PivotStats* 
 
 // CTAs 1 .. of a whole-GPU launch: wait for a job, run it, until CTA 0 posts the exit.
 template <typename FT>
-__device__ void gridWorker(GridCtl* g, const DevSettings& st) {
+__device__ __noinline__ void gridWorker(GridCtl* g, const DevSettings& st) {
   for (;;) {
     if (!gridSync(g)) return;
     volatile GridCtl* vg = g;
@@ -1296,7 +1381,7 @@ __device__ bool gridPost(Ctx& c, const DevSettings& st, int op, T* M, T* y, doub
 // ------------------------------------------------------------------------------------------
 // Builds the root for the current cone scaling with extra diagonal bumps (ep on x rows, -ea on
 // all cone rows, the regularisation ladder of kkt_system.cpp:152-168) and factors it in T.
-template <typename T>
+template <typename T, bool G = false>
 __device__ __noinline__ void assembleFactor(Ctx& c, const DevSettings& st, T* M, double ep, double ea,
                                int& fail, int& wrongSign, double& minAbsD) {
   const InstanceDesc& D = *c.D;
@@ -1319,7 +1404,7 @@ __device__ __noinline__ void assembleFactor(Ctx& c, const DevSettings& st, T* M,
       for (int k = a0; k < a1; k += d) socApplyG(c.sp[b], c.cu + off, d, c.Ad + k, c.T + k);
     }
   }
-  if (c.grid) {
+  if constexpr (G) {
     // whole-GPU launch: the assembly and the LDL' run on every CTA
     PivotStats* ps = reinterpret_cast<PivotStats*>(c.sc + SC_COUNT);
     if (threadIdx.x == 0) {
@@ -1330,7 +1415,20 @@ __device__ __noinline__ void assembleFactor(Ctx& c, const DevSettings& st, T* M,
     }
     __syncthreads();
     const long long t1 = (st.record_timings && threadIdx.x == 0) ? clock64() : 0;
-    const bool ok = gridPost<T>(c, st, kGridOpFactor, M, (T*)nullptr, ep, ea, ps);
+    // post the job, then run its two parts here (timed separately: assembly, LDL')
+    GridCtl* g = c.grid;
+    if (threadIdx.x == 0) {
+      g->op = kGridOpFactor;
+      g->arith = ArithOf<T>::v;
+      g->M = M;
+      g->y = nullptr;
+      g->ep = ep;
+      g->ea = ea;
+    }
+    extern __shared__ __align__(16) unsigned char dynSmem[];
+    bool ok = gridSync(g) && gridAssemble<T>(g, g->ctx, st, M, ep, ea);
+    const long long t2 = (st.record_timings && threadIdx.x == 0) ? clock64() : 0;
+    ok = ok && gridLdlt<T>(g, nr, n, st, M, ps, reinterpret_cast<T*>(dynSmem + g->stageOff));
     __syncthreads();
     const bool regularized = st.linear_solver == 2;
     fail = !ok ? 1 : (regularized ? (((double)ps->nreg > 0.05 * (double)nr) ? 1 : 0) : ps->zero);
@@ -1338,8 +1436,8 @@ __device__ __noinline__ void assembleFactor(Ctx& c, const DevSettings& st, T* M,
     minAbsD = ok ? ps->minAbs : NAN;
     __syncthreads();
     if (st.record_timings && threadIdx.x == 0) {
-      timers(c)[TM_ASSEMBLE] += t1 - t0;
-      timers(c)[TM_LDLT] += clock64() - t1;
+      timers(c)[TM_ASSEMBLE] += (t1 - t0) + (t2 - t1);
+      timers(c)[TM_LDLT] += clock64() - t2;
     }
     return;
   }
@@ -1373,7 +1471,7 @@ __device__ __noinline__ void assembleFactor(Ctx& c, const DevSettings& st, T* M,
 }
 
 // sol = Kreg^-1 rhs through the factored root (T) with the bump ea used at factorisation.
-template <typename T>
+template <typename T, bool G = false>
 __device__ __noinline__ void reducedSolve(Ctx& c, const DevSettings& st, const T* M, double ea,
                              const double* rhs, double* sol) {
   const int n = c.n, m = c.m, p = c.p, nr = c.nr;
@@ -1396,7 +1494,7 @@ __device__ __noinline__ void reducedSolve(Ctx& c, const DevSettings& st, const T
   for (int i = nr + (int)threadIdx.x; i < rootTiles(nr) * kTile; i += blockDim.x) y[i] = (T)0;
   __syncthreads();
   const long long t0 = (st.record_timings && threadIdx.x == 0) ? clock64() : 0;
-  if (c.grid) {
+  if constexpr (G) {
     // whole-GPU launch; a failed barrier leaves a non-finite solution, which the caller's
     // finiteness test turns into NumericalError
     if (!gridPost<T>(c, st, kGridOpSolve, const_cast<T*>(M), y, 0.0, 0.0, nullptr) && threadIdx.x == 0)
@@ -1453,14 +1551,14 @@ __device__ __forceinline__ typename HighT<FT>::type* rootHigh(Ctx& c) {
 
 // factorizeWithRetry (kkt_system.cpp:242-264) on the reduced system. In MIXED precision an FP32
 // factor with a wrong-signed pivot is replaced by the double-float factor (sticky).
-template <typename FT>
+template <typename FT, bool G = false>
 __device__ __noinline__ bool factorizeWithRetryImpl(Ctx& c, const DevSettings& st, FactState& fs) {
   double ep = 0.0, ea = 0.0;
   for (int attempt = 0; attempt < 18; ++attempt) {
     int fail = 0, wrong = 0;
     double mind = 0.0;
     if (!fs.use64) {
-      assembleFactor<FT>(c, st, rootT<FT>(c), ep, ea, fail, wrong, mind);
+      assembleFactor<FT, G>(c, st, rootT<FT>(c), ep, ea, fail, wrong, mind);
       if (sizeof(FT) == 4 && (wrong || !isfinite(mind))) {
         fs.use64 = 1;
         if (threadIdx.x == 0) c.sc[SC_NFB] += 1.0;
@@ -1468,7 +1566,7 @@ __device__ __noinline__ bool factorizeWithRetryImpl(Ctx& c, const DevSettings& s
         continue;
       }
     } else {
-      assembleFactor<typename HighT<FT>::type>(c, st, rootHigh<FT>(c), ep, ea, fail, wrong, mind);
+      assembleFactor<typename HighT<FT>::type, G>(c, st, rootHigh<FT>(c), ep, ea, fail, wrong, mind);
     }
     if (threadIdx.x == 0) c.sc[SC_ATTEMPTS] += 1.0;
     if (!fail && isfinite(mind) && mind > st.dynamic_reg_eps) {
@@ -1482,12 +1580,12 @@ __device__ __noinline__ bool factorizeWithRetryImpl(Ctx& c, const DevSettings& s
   return false;
 }
 
-template <typename FT>
+template <typename FT, bool G = false>
 __device__ void solveOnce(Ctx& c, const DevSettings& st, const FactState& fs, const double* rhs, double* sol) {
   if (fs.use64)
-    reducedSolve<typename HighT<FT>::type>(c, st, rootHigh<FT>(c), fs.ea, rhs, sol);
+    reducedSolve<typename HighT<FT>::type, G>(c, st, rootHigh<FT>(c), fs.ea, rhs, sol);
   else
-    reducedSolve<FT>(c, st, rootT<FT>(c), fs.ea, rhs, sol);
+    reducedSolve<FT, G>(c, st, rootT<FT>(c), fs.ea, rhs, sol);
 }
 
 static __device__ __noinline__ bool vecFinite(Ctx& c, const double* v, int len) {
@@ -1498,14 +1596,14 @@ static __device__ __noinline__ bool vecFinite(Ctx& c, const double* v, int len) 
 
 // KktSystem::solve (kkt_system.cpp:296-311) incl. escalateAndResolve (:266-294), plus the
 // MIXED-precision fallback to the double-float factor. Returns the final relative residual.
-template <typename FT>
+template <typename FT, bool G = false>
 __device__ bool factorizeWithRetry(Ctx& c, const DevSettings& st, FactState& fs);
 
-template <typename FT>
+template <typename FT, bool G = false>
 __device__ __noinline__ double kktSolveImpl(Ctx& c, const DevSettings& st, FactState& fs, const double* rhs, double* sol) {
   const int N = c.n + c.m;
   for (int pass = 0; pass < 2; ++pass) {
-    solveOnce<FT>(c, st, fs, rhs, sol);
+    solveOnce<FT, G>(c, st, fs, rhs, sol);
     if (!vecFinite(c, sol, N)) {
       // escalate: x1000 bumps from the held factor's, up to 10 times
       double ep = fs.ep, ea = fs.ea;
@@ -1516,13 +1614,13 @@ __device__ __noinline__ double kktSolveImpl(Ctx& c, const DevSettings& st, FactS
         int fail = 0, wrong = 0;
         double mind = 0.0;
         if (fs.use64)
-          assembleFactor<typename HighT<FT>::type>(c, st, rootHigh<FT>(c), ep, ea, fail, wrong, mind);
+          assembleFactor<typename HighT<FT>::type, G>(c, st, rootHigh<FT>(c), ep, ea, fail, wrong, mind);
         else
-          assembleFactor<FT>(c, st, rootT<FT>(c), ep, ea, fail, wrong, mind);
+          assembleFactor<FT, G>(c, st, rootT<FT>(c), ep, ea, fail, wrong, mind);
         if (fail || !isfinite(mind) || !(mind > st.dynamic_reg_eps)) continue;
         fs.ep = ep;
         fs.ea = ea;
-        solveOnce<FT>(c, st, fs, rhs, sol);
+        solveOnce<FT, G>(c, st, fs, rhs, sol);
         ok = vecFinite(c, sol, N);
       }
     }
@@ -1532,7 +1630,7 @@ __device__ __noinline__ double kktSolveImpl(Ctx& c, const DevSettings& st, FactS
     const int maxRef = fp32Factor ? st.mixed_refine_max_iter : st.refine_max_iter;
     int steps = 0;
     for (int it = 0; it < maxRef && rel > st.refine_tol; ++it) {
-      solveOnce<FT>(c, st, fs, c.res, c.cor);
+      solveOnce<FT, G>(c, st, fs, c.res, c.cor);
       FOR_T(i, N) sol[i] += c.cor[i];
       __syncthreads();
       const double prev = rel;
@@ -1556,7 +1654,7 @@ __device__ __noinline__ double kktSolveImpl(Ctx& c, const DevSettings& st, FactS
       // sticky fallback: refactor in double-float (with the retry ladder) and redo this solve
       fs.use64 = 1;
       if (threadIdx.x == 0) c.sc[SC_NFB] += 1.0;
-      if (!factorizeWithRetry<FT>(c, st, fs)) return INFINITY;
+      if (!factorizeWithRetry<FT, G>(c, st, fs)) return INFINITY;
       continue;
     }
     if (threadIdx.x == 0) {
@@ -1568,19 +1666,19 @@ __device__ __noinline__ double kktSolveImpl(Ctx& c, const DevSettings& st, FactS
   return INFINITY;
 }
 
-template <typename FT>
+template <typename FT, bool G>
 __device__ bool factorizeWithRetry(Ctx& c, const DevSettings& st, FactState& fs) {
   const long long t0 = st.record_timings ? clock64() : 0;
-  const bool ok = factorizeWithRetryImpl<FT>(c, st, fs);
+  const bool ok = factorizeWithRetryImpl<FT, G>(c, st, fs);
   if (st.record_timings && threadIdx.x == 0) timers(c)[TM_FACTOR] += clock64() - t0;
   return ok;
 }
 
-template <typename FT>
+template <typename FT, bool G = false>
 __device__ double kktSolve(Ctx& c, const DevSettings& st, FactState& fs, const double* rhs, double* sol) {
   const long long t0 = st.record_timings ? clock64() : 0;
   // the fallback path inside refactors; its time is counted as solve time
-  const double r = kktSolveImpl<FT>(c, st, fs, rhs, sol);
+  const double r = kktSolveImpl<FT, G>(c, st, fs, rhs, sol);
   if (st.record_timings && threadIdx.x == 0) timers(c)[TM_SOLVE] += clock64() - t0;
   return r;
 }
@@ -1588,7 +1686,7 @@ __device__ double kktSolve(Ctx& c, const DevSettings& st, FactState& fs, const d
 // ------------------------------------------------------------------------------------------
 // the IPM driver for one instance (solver_impl.cpp SolverImpl::solve and helpers)
 // ------------------------------------------------------------------------------------------
-template <typename FT>
+template <typename FT, bool G = false>
 __device__ __noinline__ void solveInstance(Ctx& c, const LaunchArgs& a, int inst) {
   const DevSettings& st = a.st;
   const InstanceDesc& D = *c.D;
@@ -1620,26 +1718,26 @@ __device__ __noinline__ void solveInstance(Ctx& c, const LaunchArgs& a, int inst
   } else {
     // computeInitialPoint: Hs = I scaling of the identity element, 1 or 2 KKT solves
     coneUpdateScaling(c, c.ev, c.ev);
-    if (!factorizeWithRetry<FT>(c, st, fs)) {
+    if (!factorizeWithRetry<FT, G>(c, st, fs)) {
       initOk = false;
     } else {
       if (D.pStoredNnz == 0) {
         FOR_T(j, n) c.rhs[j] = 0.0;
         FOR_T(r, m) c.rhs[n + r] = c.bs[r];
         __syncthreads();
-        kktSolve<FT>(c, st, fs, c.rhs, c.sol);
+        kktSolve<FT, G>(c, st, fs, c.rhs, c.sol);
         FOR_T(j, n) c.x[j] = c.sol[j];
         FOR_T(r, m) c.s[r] = -c.sol[n + r];
         FOR_T(j, n) c.rhs[j] = -c.qs[j];
         FOR_T(r, m) c.rhs[n + r] = 0.0;
         __syncthreads();
-        kktSolve<FT>(c, st, fs, c.rhs, c.sol);
+        kktSolve<FT, G>(c, st, fs, c.rhs, c.sol);
         FOR_T(r, m) c.z[r] = c.sol[n + r];
       } else {
         FOR_T(j, n) c.rhs[j] = -c.qs[j];
         FOR_T(r, m) c.rhs[n + r] = c.bs[r];
         __syncthreads();
-        kktSolve<FT>(c, st, fs, c.rhs, c.sol);
+        kktSolve<FT, G>(c, st, fs, c.rhs, c.sol);
         FOR_T(j, n) c.x[j] = c.sol[j];
         FOR_T(r, m) {
           c.z[r] = c.sol[n + r];
@@ -1663,12 +1761,12 @@ __device__ __noinline__ void solveInstance(Ctx& c, const LaunchArgs& a, int inst
     iterations = iter + 1;
     // 1. refactorise for the current scaling
     coneUpdateScaling(c, c.s, c.z);
-    if (!factorizeWithRetry<FT>(c, st, fs)) { status = 5; break; }
+    if (!factorizeWithRetry<FT, G>(c, st, fs)) { status = 5; break; }
     // 2. constant solve (-q, b) -> x1, z1; Px1
     FOR_T(j, n) c.rhs[j] = -c.qs[j];
     FOR_T(r, m) c.rhs[n + r] = c.bs[r];
     __syncthreads();
-    kktSolve<FT>(c, st, fs, c.rhs, c.sol);
+    kktSolve<FT, G>(c, st, fs, c.rhs, c.sol);
     FOR_T(j, n) c.x1[j] = c.sol[j];
     FOR_T(r, m) c.z1[r] = c.sol[n + r];
     __syncthreads();
@@ -1740,7 +1838,7 @@ __device__ __noinline__ void solveInstance(Ctx& c, const LaunchArgs& a, int inst
       FOR_T(j, n) c.rhs[j] = c.rx[j];
       FOR_T(r, m) c.rhs[n + r] = c.s[r] - c.rz[r];
       __syncthreads();
-      kktSolve<FT>(c, st, fs, c.rhs, c.sol);
+      kktSolve<FT, G>(c, st, fs, c.rhs, c.sol);
       if (!vecFinite(c, c.sol, N)) { status = 5; break; }
       pmul(c, c.sol, c.tn);  // P xv
       double tn3[3] = {0, 0, 0};
@@ -1798,7 +1896,7 @@ __device__ __noinline__ void solveInstance(Ctx& c, const LaunchArgs& a, int inst
       FOR_T(j, n) c.rhs[j] = (1.0 - sigma) * c.rx[j];
       FOR_T(r, m) c.rhs[n + r] = c.dcon[r] - (1.0 - sigma) * c.rz[r];
       __syncthreads();
-      kktSolve<FT>(c, st, fs, c.rhs, c.sol);
+      kktSolve<FT, G>(c, st, fs, c.rhs, c.sol);
       if (!vecFinite(c, c.sol, N)) { status = 5; break; }
       pmul(c, c.sol, c.tn);
       tn3[0] = tn3[1] = tn3[2] = 0.0;
@@ -1930,7 +2028,7 @@ __device__ __noinline__ void solveInstance(Ctx& c, const LaunchArgs& a, int inst
     R.fp64_fallbacks = (int)c.sc[SC_NFB];
     R.refine_steps = (int)c.sc[SC_RSTEPS];
     R.factor_attempts = (int)c.sc[SC_ATTEMPTS];
-    R.error_code = (c.grid && reinterpret_cast<volatile GridCtl*>(c.grid)->error) ? 1 : 0;
+    R.error_code = (G && reinterpret_cast<volatile GridCtl*>(c.grid)->error) ? 1 : 0;
     const long long tot = clock64() - tStart;
     R.cycles[0] = tot;
     if (st.record_timings) {
@@ -2005,39 +2103,13 @@ static __device__ void setupCtx(Ctx& c, const LaunchArgs& a, int inst, unsigned 
 // kMaxThreads / kMinBlocks: the large-root form (up to 256 threads, registers for one CTA per
 // SM) and the small-root form (up to 64 threads, at least 8 CTAs per SM: small instances are
 // bound by FP64 latency, so more of them resident per SM is more throughput).
-//
-// Whole-GPU form (a.grid set; large-root form only): one large instance, a cooperative launch
-// with one CTA per SM. CTA 0 runs the iteration, the other CTAs run the root jobs it posts (see
-// gridSync); the vectors, the root and the solve vector are in CTA 0's scratch (global memory)
-// so every CTA can reach them.
+
 template <typename FT, int kMaxThreads, int kMinBlocks>
 __global__ void __launch_bounds__(kMaxThreads, kMinBlocks) ipmKernel(LaunchArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ int sInst;
   __shared__ int sRedi[4];
   __shared__ Ctx c;
-  if constexpr (kMaxThreads >= 256) {
-    if (a.grid) {
-      GridCtl* g = a.grid;
-      if (blockIdx.x == 0) {
-        const int inst = a.order[0];
-        if (threadIdx.x == 0) {
-          setupCtx(c, a, inst, smem, a.scratch, sRedi);
-          c.grid = g;
-          g->ctx = c;
-          g->stageOff = a.lay.rootOff;  // the root itself is in scratch in this form
-        }
-        __syncthreads();
-        loadInstance(c, a);
-        solveInstance<FT>(c, a, inst);
-        if (threadIdx.x == 0) g->op = kGridOpExit;
-        gridSync(g);
-      } else {
-        gridWorker<FT>(g, a.st);
-      }
-      return;
-    }
-  }
   double* scratch = a.scratch + (int64_t)blockIdx.x * a.scratchStride;
   for (;;) {
     if (threadIdx.x == 0) sInst = atomicAdd(a.counter, 1);
@@ -2050,6 +2122,34 @@ __global__ void __launch_bounds__(kMaxThreads, kMinBlocks) ipmKernel(LaunchArgs 
     __syncthreads();
     loadInstance(c, a);
     solveInstance<FT>(c, a, inst);
+  }
+}
+
+// Whole-GPU form for one large instance (a.grid set): a cooperative launch with one CTA per SM.
+// CTA 0 runs the iteration, the other CTAs run the root jobs it posts (see gridSync); the
+// vectors, the root and the solve vector are in CTA 0's scratch (global memory) so every CTA can
+// reach them. A kernel of its own, so that the batched kernels keep their register allocation.
+template <typename FT>
+__global__ void __launch_bounds__(256, 1) ipmGridKernel(LaunchArgs a) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ int sRedi[4];
+  __shared__ Ctx c;
+  GridCtl* g = a.grid;
+  if (blockIdx.x == 0) {
+    const int inst = a.order[0];
+    if (threadIdx.x == 0) {
+      setupCtx(c, a, inst, smem, a.scratch, sRedi);
+      c.grid = g;
+      g->ctx = c;
+      g->stageOff = a.lay.rootOff;  // the root itself is in scratch in this form
+    }
+    __syncthreads();
+    loadInstance(c, a);
+    solveInstance<FT, true>(c, a, inst);
+    if (threadIdx.x == 0) g->op = kGridOpExit;
+    gridSync(g);
+  } else {
+    gridWorker<FT>(g, a.st);
   }
 }
 
@@ -2115,8 +2215,8 @@ static __device__ __noinline__ void adjointInstance(Ctx& c, const LaunchArgs& a)
 
 
 // Host launchers of the kernels above, per root arithmetic FT (float: mixed precision, double:
-// FP64) and launch form; explicitly instantiated in cxg_ipm_f32.cu, cxg_ipm_f32s.cu and
-// cxg_ipm_f64.cu.
+// FP64) and launch form; explicitly instantiated in cxg_ipm_f32.cu, cxg_ipm_f32s.cu,
+// cxg_ipm_f64.cu (batched forms) and cxg_ipm_gridf.cu, cxg_ipm_gridd.cu (whole-GPU form).
 template <typename FT, int kMaxThreads, int kMinBlocks>
 cudaError_t launchIpmFormT(const LaunchArgs& a, int grid, int block, size_t smem, cudaStream_t stream) {
   void (*k)(LaunchArgs) = ipmKernel<FT, kMaxThreads, kMinBlocks>;
@@ -2136,7 +2236,7 @@ cudaError_t ipmOccupancyFormT(int* blocksPerSM, int block, size_t smem) {
 
 template <typename FT>
 cudaError_t launchIpmGridT(const LaunchArgs& a, GridCtl* g, int grid, size_t smem, cudaStream_t stream) {
-  void (*k)(LaunchArgs) = ipmKernel<FT, 256, 1>;
+  void (*k)(LaunchArgs) = ipmGridKernel<FT>;
   cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   LaunchArgs av = a;
@@ -2147,7 +2247,10 @@ cudaError_t launchIpmGridT(const LaunchArgs& a, GridCtl* g, int grid, size_t sme
 
 template <typename FT>
 cudaError_t ipmGridOccupancyT(int* blocksPerSM, size_t smem) {
-  return ipmOccupancyFormT<FT, 256, 1>(blocksPerSM, 256, smem);
+  void (*k)(LaunchArgs) = ipmGridKernel<FT>;
+  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocksPerSM, k, 256, smem);
 }
 
 // Explicit instantiation (EXT empty) or declaration (EXT extern) of the launchers of one form.

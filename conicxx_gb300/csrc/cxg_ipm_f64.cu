@@ -6,11 +6,11 @@ namespace cxg {
 
 CXG_IPM_FORM(, double, 256, 1)
 CXG_IPM_FORM(, double, 64, 8)
-CXG_IPM_GRID(, double)
-// instantiated in cxg_ipm_f32.cu and cxg_ipm_f32s.cu
+// instantiated in cxg_ipm_f32.cu, cxg_ipm_f32s.cu, cxg_ipm_gridf.cu and cxg_ipm_gridd.cu
 CXG_IPM_FORM(extern, float, 256, 1)
 CXG_IPM_FORM(extern, float, 64, 8)
 CXG_IPM_GRID(extern, float)
+CXG_IPM_GRID(extern, double)
 
 size_t gridCtlBytes() { return sizeof(GridCtl); }
 

@@ -96,9 +96,11 @@ typedef struct cxg_settings {
   int differentiable;         /* keep each instance's final factorisation, scaling and iterate on the
                                  device so backward() can reuse them (default 0; cxg_solver: 1);
                                  ignored for whole-GPU roots above 8192 rows */
-  int whole_gpu_root;         /* single-instance handles (count 1): 0 = automatic, the root is spread
-                                 over every SM when it has more than 512 rows (always beyond 4096);
-                                 1 = always; -1 = never (one CTA, roots up to 4096 rows) */
+  int whole_gpu_root;         /* one instance (cxg_solver, or a batch of count 1): 1 = spread the root
+                                 over every SM (cooperative launch, roots up to 131072 rows); -1 =
+                                 never (one CTA, roots up to 4096 rows); 0 = automatic: cxg_solver
+                                 spreads roots of more than 512 rows, a batch of one only roots of
+                                 more than 4096 */
 } cxg_settings;
 
 /* conicxx::Info (include/conicxx/solution.h:18-26) plus Solution::objective/status and counters. */
