@@ -1,4 +1,5 @@
-// Launch interface of the device kernels (cxg_ipm.cu, cxg_adjoint.cu) as seen by the host API.
+// Launch interface of the device kernels (cxg_ipm.cuh and its instantiations cxg_ipm_*.cu) as seen by
+// the host API.
 #pragma once
 
 #include <cuda_runtime.h>

@@ -1,5 +1,5 @@
 // Layout of one problem instance on the device, shared by the host planner (cxg_plan.cpp)
-// and the interior-point kernel (cxg_ipm.cu).
+// and the interior-point kernel (cxg_ipm.cuh).
 //
 // The KKT system of ConicXX (src/conicxx/kkt/kkt_system.h:18-65)
 //     K = [ P + epsP I      A'           ]
