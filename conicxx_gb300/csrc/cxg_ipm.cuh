@@ -1072,21 +1072,37 @@ __device__ __forceinline__ void lds4(const T* p, T (&v)[4]) {
 
 // C -= A D B^T for one super-block of up to 4x4 tiles, by one CTA of 256 threads:
 // rows I0 .. I0+ni-1 and columns K0 .. K0+nk-1 (tile indices); only tiles with column <= row when
-// the super-block is on the diagonal. A = the panel tiles L_IJ, B = L_KJ, D = diag of tile (J, J).
-// The panel is staged k-major in shared memory (B pre-scaled by D exactly as tileSyrk scales
-// it), each thread accumulates an 8x8 block of the 128x128 product over k = 0..31 in the order
-// tileSyrk uses (so every entry gets the same bits), the results go to shared memory in tile
-// layout, and the C tiles are updated with 16-byte vector loads and stores.
+// the super-block is on the diagonal, and not its first tile when skip00 (updated elsewhere).
+// A = the panel tiles L_IJ, B = L_KJ, D = diag of tile (J, J).
+// The C tiles are copied into shared memory asynchronously (cp.async) while the panel is staged
+// k-major (B pre-scaled by D exactly as tileSyrk scales it) and each thread accumulates an 8x8
+// block of the 128x128 product over k = 0..31 in the order tileSyrk uses; then C -= product in
+// shared memory (so every entry gets the same bits as tileSyrk) and the tiles are stored back
+// with 16-byte vectors.
 template <typename T>
-__device__ __noinline__ void superSyrk(T* M, int Tn, int J, int I0, int K0, int ni, int nk, bool diagSb, T* sm) {
+__device__ __noinline__ void superSyrk(T* M, int Tn, int J, int I0, int K0, int ni, int nk, bool diagSb, bool skip00,
+                                      T* sm) {
   T* As = sm;
   T* Bs = sm + kTile * kSbDim;
   T* Cs = sm + 2 * kTile * kSbDim;
   const T* Ajj = M + tileBase(Tn, J, J);
   const int tid = threadIdx.x;
+  constexpr int per16 = 16 / (int)sizeof(T);
+  constexpr int vpt = kTileElems / per16;  // 16-byte vectors per tile
+  // (1) the C tiles of this super-block, global -> Cs, as asynchronous 16-byte copies that
+  //     proceed while the panel is staged and the product computed
+  for (int v = tid; v < 16 * vpt; v += blockDim.x) {
+    const int t = v / vpt, a = t >> 2, b = t & 3;
+    if (a < ni && b < nk && !(diagSb && b > a) && !(skip00 && t == 0)) {
+      const T* src = M + tileBase(Tn, I0 + a, K0 + b) + (v - t * vpt) * per16;
+      const unsigned dst = (unsigned)__cvta_generic_to_shared(Cs + v * per16);
+      asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(dst), "l"(src) : "memory");
+    }
+  }
+  asm volatile("cp.async.commit_group;\n" ::: "memory");
   {
-    // thread tid stages column i = tid & 127 of the panel for k = tid >> 7, +2, ... (all loads of
-    // the thread issued before any store, so their latencies overlap)
+    // (2) the panel: thread tid stages column i = tid & 127 for k = tid >> 7, +2, ... (all loads
+    //     of a half issued before any store, so their latencies overlap)
     const int i = tid & (kSbDim - 1), a = i >> 5, rr = i & 31, k0 = tid >> 7;
     const T* pa = (a < ni) ? M + tileBase(Tn, I0 + a, J) + rr : nullptr;
     const T* pb = (a < nk) ? M + tileBase(Tn, K0 + a, J) + rr : nullptr;
@@ -1110,6 +1126,7 @@ __device__ __noinline__ void superSyrk(T* M, int Tn, int J, int I0, int K0, int 
     }
   }
   __syncthreads();
+  // (3) the product, 8x8 per thread, k = 0..31 in the tile routine's order
   const int tx = tid & 15, ty = tid >> 4;  // rows tx*4 + {0..3, 64..67}, columns ty*4 + {0..3, 64..67}
   T acc[8][8];
 #pragma unroll
@@ -1133,54 +1150,35 @@ __device__ __noinline__ void superSyrk(T* M, int Tn, int J, int I0, int K0, int 
         acc[4 + i][4 + j] = accT(acc[4 + i][4 + j], a1[i], b1[j]);
       }
   }
-  // results to shared memory in tile layout (tile t = a * 4 + b), padding entries zeroed
+  // (4) C -= product in shared memory (each thread its own 64 entries of the copied C tiles;
+  //     entries of tiles that are not updated are never stored back)
+  asm volatile("cp.async.wait_all;\n" ::: "memory");
+  __syncthreads();
 #pragma unroll
   for (int i = 0; i < 8; ++i) {
     const int R = (i < 4) ? tx * 4 + i : 64 + tx * 4 + (i - 4);
 #pragma unroll
     for (int j = 0; j < 8; ++j) {
       const int Cc = (j < 4) ? ty * 4 + j : 64 + ty * 4 + (j - 4);
-      Cs[((R >> 5) * 4 + (Cc >> 5)) * kTileElems + (Cc & 31) * kTileLd + (R & 31)] = accEnd(acc[i][j]);
+      T& cref = Cs[((R >> 5) * 4 + (Cc >> 5)) * kTileElems + (Cc & 31) * kTileLd + (R & 31)];
+      cref = cref - accEnd(acc[i][j]);
     }
   }
-  for (int idx = tid; idx < 16 * kTile; idx += blockDim.x) Cs[(idx >> 5) * kTileElems + (idx & 31) * kTileLd + 32] = (T)0;
   __syncthreads();
-  // C -= result, 16-byte vectors; each thread loads a batch of its vectors before storing any
-  constexpr int per16 = 16 / (int)sizeof(T);
-  constexpr int vpt = kTileElems / per16;  // vectors per tile
-  constexpr int kBatch = 4;
-  const int total = 16 * vpt;
-  for (int base = 0; base < total; base += kBatch * (int)blockDim.x) {
-    uint4 cv[kBatch];
-    T* cp[kBatch];
-#pragma unroll
-    for (int u = 0; u < kBatch; ++u) {
-      const int v = base + u * (int)blockDim.x + tid;
-      const int t = v / vpt, a = t >> 2, b = t & 3;
-      const bool use = v < total && a < ni && b < nk && !(diagSb && b > a);
-      cp[u] = use ? M + tileBase(Tn, I0 + a, K0 + b) + (v - t * vpt) * per16 : nullptr;
-      if (use) cv[u] = *reinterpret_cast<const uint4*>(cp[u]);
-    }
-#pragma unroll
-    for (int u = 0; u < kBatch; ++u) {
-      if (!cp[u]) continue;
-      const int v = base + u * (int)blockDim.x + tid;
-      alignas(16) T c[per16];
-      alignas(16) T d[per16];
-      *reinterpret_cast<uint4*>(c) = cv[u];
-      *reinterpret_cast<uint4*>(d) = *reinterpret_cast<const uint4*>(Cs + v * per16);
-#pragma unroll
-      for (int e = 0; e < per16; ++e) c[e] = c[e] - d[e];
-      *reinterpret_cast<uint4*>(cp[u]) = *reinterpret_cast<const uint4*>(c);
-    }
+  // (5) back to global memory, 16-byte vectors
+  for (int v = tid; v < 16 * vpt; v += blockDim.x) {
+    const int t = v / vpt, a = t >> 2, b = t & 3;
+    if (a < ni && b < nk && !(diagSb && b > a) && !(skip00 && t == 0))
+      *reinterpret_cast<uint4*>(M + tileBase(Tn, I0 + a, K0 + b) + (v - t * vpt) * per16) =
+          *reinterpret_cast<const uint4*>(Cs + v * per16);
   }
 }
 
 // Tiled right-looking LDL' of the root over the whole grid. Per tile column J:
 //  (A) the off-diagonal tiles of column J, one warp each; barrier;
 //  (B) the trailing update C_IK -= L_IJ D_J L_KJ^T, J < K <= I, in super-blocks of 4x4 tiles, one
-//      CTA each (superSyrk). CTA 0 takes the first super-block, then its warp 0 factors the tile
-//      (J+1, J+1) in the same step (one-column lookahead); barrier.
+//      CTA each (superSyrk, CTAs 1..), while warp 0 of CTA 0 updates the tile (J+1, J+1) with the
+//      tile routine and factors it (one-column lookahead); barrier.
 // Every root entry receives its updates in increasing J with the same operations and rounding as
 // the single-CTA factor, so both give the same bits. Only warp 0 of CTA 0 factors diagonal tiles,
 // so the pivot statistics stay in CTA 0's shared memory (ps). `stage` holds gridStageBytes.
@@ -1199,21 +1197,27 @@ __device__ __noinline__ bool gridLdlt(GridCtl* g, int nr, int nx, const DevSetti
     const int rem = Tn - J - 1;
     const int nb = (rem + 3) >> 2;
     const long long nsb = (long long)nb * (nb + 1) / 2;
-    // super-blocks in row order: sb = r (r + 1) / 2 + k, tile rows J+1+4r.., tile columns J+1+4k..
-    // CTA 0 takes sb = 0 only; CTAs 1.. take 1, 2, ... cyclically
-    const long long step = cta0 ? nsb : (long long)gridDim.x - 1;
-    for (long long sb = cta0 ? 0 : (long long)blockIdx.x; sb < nsb; sb += step) {
+    // CTA 0's warp 0 updates and factors the next diagonal tile (J+1, J+1), the critical path of
+    // the next column; the super-blocks (row order: sb = r (r + 1) / 2 + k, tile rows J+1+4r..,
+    // tile columns J+1+4k..) go to CTAs 1.. cyclically, super-block 0 without that tile
+    if (cta0) {
+      if (warp == 0) {
+        T* An = M + tileBase(Tn, J + 1, J + 1);
+        const T* Ln = M + tileBase(Tn, J + 1, J);
+        tileSyrk<T>(An, Ln, Ln, Ajj);
+        tileFactorDiag<T>(An, J + 1, nr, nx, st, ps);
+      }
+      if (!gridSync(g)) return false;
+      continue;
+    }
+    for (long long sb = (long long)blockIdx.x - 1; sb < nsb; sb += (long long)gridDim.x - 1) {
       int r = (int)((sqrtf(8.0f * (float)sb + 1.0f) - 1.0f) * 0.5f);
       while ((long long)r * (r + 1) / 2 > sb) --r;
       while ((long long)(r + 1) * (r + 2) / 2 <= sb) ++r;
       const int k = (int)(sb - (long long)r * (r + 1) / 2);
       const int I0 = J + 1 + 4 * r, K0 = J + 1 + 4 * k;
       __syncthreads();  // the previous super-block is done with the staging area
-      superSyrk<T>(M, Tn, J, I0, K0, min(4, Tn - I0), min(4, Tn - K0), r == k, stage);
-      if (cta0) {
-        __syncthreads();
-        if (warp == 0) tileFactorDiag<T>(M + tileBase(Tn, J + 1, J + 1), J + 1, nr, nx, st, ps);
-      }
+      superSyrk<T>(M, Tn, J, I0, K0, min(4, Tn - I0), min(4, Tn - K0), r == k, sb == 0, stage);
     }
     if (!gridSync(g)) return false;
   }
