@@ -1284,49 +1284,104 @@ __device__ __forceinline__ void warpRowsBackward(const T* Ljk, const T* xJ, T* y
   yK[lane] = yK[lane] - accEnd(acc);
 }
 
-// y <- M^-1 y over the grid. Forward step J: CTA 0 updates tile J+1 from tile J and solves its
-// diagonal block (lookahead), scales the finished tile J-1 by D, while the warps of the other
-// CTAs update tiles J+2 ... from tile J; one barrier per step. The backward pass mirrors it.
-// Needs at least two CTAs.
+// y <- M^-1 y over the grid, in blocks of kSolveBlk tiles (one barrier per block step).
+// Forward step B: warps 0..3 of CTA 0 update the tiles of block B+1 from block B, warp 4 scales
+// block B-1 (finished) by D, then CTA 0 solves block B+1 within itself (ctaBlockForward, CTA
+// barriers only); meanwhile the warps of the other CTAs update
+// every tile of blocks B+2.. from block B, one tile each. The backward pass mirrors it. Each
+// y tile receives its updates one source tile at a time, in increasing (forward) / decreasing
+// (backward) source order. Needs at least two CTAs.
+constexpr int kSolveBlk = 4;
+
+// Solve of one block of tiles b0 .. b1-1 within itself by the calling CTA: per tile j, the
+// diagonal block (ctaDiag*) then the updates of the block's other tiles from tile j, one warp
+// each, with CTA barriers only.
+template <typename T>
+__device__ void ctaBlockForward(const T* M, int Tn, int b0, int b1, T* y) {
+  const int warp = threadIdx.x >> 5;
+  for (int j = b0; j < b1; ++j) {
+    ctaDiagForward<T>(M + tileBase(Tn, j, j), y + j * 32);
+    const int i = j + 1 + warp;
+    if (i < b1) warpRowsForward<T>(M + tileBase(Tn, i, j), y + j * 32, y + i * 32);
+    __syncthreads();
+  }
+}
+
+template <typename T>
+__device__ void ctaBlockBackward(const T* M, int Tn, int b0, int b1, T* y) {
+  const int warp = threadIdx.x >> 5;
+  for (int j = b1 - 1; j >= b0; --j) {
+    ctaDiagBackward<T>(M + tileBase(Tn, j, j), y + j * 32);
+    const int k = j - 1 - warp;
+    if (k >= b0) warpRowsBackward<T>(M + tileBase(Tn, j, k), y + j * 32, y + k * 32);
+    __syncthreads();
+  }
+}
+
 template <typename T>
 __device__ __noinline__ bool gridSolve(GridCtl* g, int nr, const T* M, T* y) {
   const int Tn = rootTiles(nr);
+  const int NB = (Tn + kSolveBlk - 1) / kSolveBlk;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, W = blockDim.x >> 5;
   const bool drv = blockIdx.x == 0;
   const int ww = ((int)blockIdx.x - 1) * W + warp, WW = ((int)gridDim.x - 1) * W;
-  auto scaleTile = [&](int J) {
-    T* yJ = y + J * 32;
-    yJ[lane] /= M[tileBase(Tn, J, J) + lane * kTileLd + lane];
+  auto blo = [&](int B) { return B * kSolveBlk; };
+  auto bhi = [&](int B) { return min(Tn, (B + 1) * kSolveBlk); };
+  auto scaleBlock = [&](int B) {  // one warp
+    for (int j = blo(B); j < bhi(B); ++j) y[j * 32 + lane] /= M[tileBase(Tn, j, j) + lane * kTileLd + lane];
   };
-  if (drv) ctaDiagForward<T>(M, y);
+  // forward
+  if (drv) ctaBlockForward<T>(M, Tn, blo(0), bhi(0), y);
   if (!gridSync(g)) return false;
-  for (int J = 0; J + 1 < Tn; ++J) {
-    const T* yJ = y + J * 32;
+  for (int B = 0; B + 1 < NB; ++B) {
     if (drv) {
-      if (warp == 0) warpRowsForward<T>(M + tileBase(Tn, J + 1, J), yJ, y + (J + 1) * 32);
-      else if (warp == 1 && J >= 1) scaleTile(J - 1);
+      const int I = blo(B + 1) + warp;
+      if (warp < kSolveBlk && I < bhi(B + 1)) {
+        for (int j = blo(B); j < bhi(B); ++j) {
+          warpRowsForward<T>(M + tileBase(Tn, I, j), y + j * 32, y + I * 32);
+          __syncwarp();
+        }
+      } else if (warp == kSolveBlk && B >= 1) {
+        scaleBlock(B - 1);
+      }
       __syncthreads();
-      ctaDiagForward<T>(M + tileBase(Tn, J + 1, J + 1), y + (J + 1) * 32);
+      ctaBlockForward<T>(M, Tn, blo(B + 1), bhi(B + 1), y);
     } else {
-      for (int I = J + 2 + ww; I < Tn; I += WW) warpRowsForward<T>(M + tileBase(Tn, I, J), yJ, y + I * 32);
+      for (int I = blo(B + 2) + ww; I < Tn; I += WW) {
+        for (int j = blo(B); j < bhi(B); ++j) {
+          warpRowsForward<T>(M + tileBase(Tn, I, j), y + j * 32, y + I * 32);
+          __syncwarp();
+        }
+      }
     }
     if (!gridSync(g)) return false;
   }
+  // backward
   if (drv) {
-    // tiles Tn-2 and Tn-1 are not scaled yet (the forward steps scale tiles up to Tn-3)
-    if (warp < 2 && Tn - 1 - warp >= 0) scaleTile(Tn - 1 - warp);
+    // blocks NB-2 and NB-1 are not scaled yet (the forward steps scale blocks up to NB-3)
+    if (warp < 2 && NB - 1 - warp >= 0) scaleBlock(NB - 1 - warp);
     __syncthreads();
-    ctaDiagBackward<T>(M + tileBase(Tn, Tn - 1, Tn - 1), y + (Tn - 1) * 32);
+    ctaBlockBackward<T>(M, Tn, blo(NB - 1), bhi(NB - 1), y);
   }
   if (!gridSync(g)) return false;
-  for (int J = Tn - 1; J >= 1; --J) {
-    const T* xJ = y + J * 32;
+  for (int B = NB - 1; B >= 1; --B) {
     if (drv) {
-      if (warp == 0) warpRowsBackward<T>(M + tileBase(Tn, J, J - 1), xJ, y + (J - 1) * 32);
+      const int K = blo(B - 1) + warp;
+      if (warp < kSolveBlk && K < bhi(B - 1)) {
+        for (int j = bhi(B) - 1; j >= blo(B); --j) {
+          warpRowsBackward<T>(M + tileBase(Tn, j, K), y + j * 32, y + K * 32);
+          __syncwarp();
+        }
+      }
       __syncthreads();
-      ctaDiagBackward<T>(M + tileBase(Tn, J - 1, J - 1), y + (J - 1) * 32);
+      ctaBlockBackward<T>(M, Tn, blo(B - 1), bhi(B - 1), y);
     } else {
-      for (int K = J - 2 - ww; K >= 0; K -= WW) warpRowsBackward<T>(M + tileBase(Tn, J, K), xJ, y + K * 32);
+      for (int K = blo(B - 1) - 1 - ww; K >= 0; K -= WW) {
+        for (int j = bhi(B) - 1; j >= blo(B); --j) {
+          warpRowsBackward<T>(M + tileBase(Tn, j, K), y + j * 32, y + K * 32);
+          __syncwarp();
+        }
+      }
     }
     if (!gridSync(g)) return false;
   }
