@@ -86,6 +86,26 @@ def test_grid_factor_large_root(arith):
     assert rel(L @ np.diag(D) @ L.T, K) < tol
 
 
+@pytest.mark.parametrize("precision", [_abi.PRECISION_FP64, _abi.PRECISION_MIXED])
+@pytest.mark.parametrize("idx", range(8))
+def test_kats_whole_gpu(kats, idx, precision):
+    """Every known-answer problem through the whole-GPU form (roots of one tile: the one-block
+    edge of the solve, and the infeasibility statuses)."""
+    from conftest import kat_qp
+    from conicxx_gb300 import Solver
+
+    k = kats[idx]
+    qp = kat_qp(k)
+    S = Solver()
+    assert S.setup(qp, precision=precision, whole_gpu_root=1)
+    sol = S.solve()
+    assert sol.status == k["status"], (k["name"], sol.status_name)
+    if k["x"] is not None:
+        assert np.allclose(sol.x, k["x"], atol=k["tol"]), (k["name"], sol.x)
+    if k["objective"] is not None:
+        assert abs(sol.objective - k["objective"]) < k["tol"]
+
+
 def _small_large_qp():
     # the large sparse QP family (P = M'M + 1e-3 I, 3 nnz per column of M; A 8 nnz per row) at
     # n = 1000, m = 1500: root of 1100 rows, 35 tile columns

@@ -129,6 +129,49 @@ def test_generators_deterministic_and_feasible():
     assert np.linalg.eigvalsh(Pd).min() > 0.5e-6
 
 
+def test_large_instance_generators():
+    """The single large-instance families: shapes, structure and the primal-dual pair construction
+    (b - A x0 interior to the cone, known from the generator's seeded draws) at reduced size, and
+    the full configuration 2 shape."""
+    qp = generators.large_sparse_qp(0, n=1000, m_zero=100, m_nonneg=1200, n_soc=100)
+    assert qp.n == 1000 and qp.m == 1500 and qp.zero == 100 and qp.nonneg == 1200 and qp.soc == [2] * 100
+    assert np.all(np.diff(qp.A.indptr) >= 0)
+    rows_per = np.bincount(qp.A.indices, minlength=qp.m)
+    assert np.all(rows_per == 8)  # 8 distinct nonzeros per row of A
+    assert np.all(qp.P.indices <= qp.P.col_of_entries())
+    Pd = qp.P.to_dense()
+    Pd = np.triu(Pd) + np.triu(Pd, 1).T
+    assert np.linalg.eigvalsh(Pd).min() > 0.9e-3  # M'M + 1e-3 I
+    a, b = generators.large_sparse_qp(0, n=300, m_zero=30, m_nonneg=360, n_soc=30), \
+        generators.large_sparse_qp(0, n=300, m_zero=30, m_nonneg=360, n_soc=30)
+    assert np.array_equal(a.A.data, b.A.data) and np.array_equal(a.q, b.q)
+    full = generators.large_sparse_qp(0)
+    assert full.n == 20000 and full.m == 30000 and full.zero == 2000 and full.nonneg == 24000
+    assert full.A.nnz == 240000
+    g = generators.group_lasso_socp(0, groups=60)
+    assert g.n == 60 * 17 and g.m == 60 * 17 and g.soc == [17] * 60 and g.zero == 0 and g.nonneg == 0
+    # each SOC block is (t_j, x_Gj): rows -e on t_j and the group's 16 x entries
+    assert g.A.nnz == 60 * 17 and np.all(g.A.data == -1.0)
+    assert np.all(g.q[60 * 16:] == 0.1)
+
+
+def test_whole_gpu_setting_rejections():
+    """Roots above the one-CTA limit are refused when the whole-GPU form is switched off or the
+    handle is a batch of several instances (host checks, no device work)."""
+    n = 4200
+    P = Csc.from_coo(n, n, np.arange(n), np.arange(n), np.ones(n))
+    A = Csc.from_coo(1, n, [0], [0], [-1.0])
+    qp = QP(P, np.zeros(n), A, np.ones(1), 0, 1, [])
+    prob, keep = make_problem_struct(qp)
+    st = _abi.default_settings(whole_gpu_root=-1)
+    h = C.c_void_p()
+    assert _lib.lib().cxg_batch_create(C.byref(h), 1, C.byref(prob), C.byref(st)) == _abi.E_UNSUPPORTED
+    assert b"4096" in _lib.lib().cxg_last_error()
+    arr = (_abi.Problem * 2)(prob, prob)
+    st = _abi.default_settings()
+    assert _lib.lib().cxg_batch_create(C.byref(h), 2, arr, C.byref(st)) == _abi.E_UNSUPPORTED
+
+
 def test_sharding_balanced():
     qps = generators.contact_batch(64)
     costs = [instance_cost(q) for q in qps]
