@@ -204,7 +204,9 @@ static int64_t r2(int64_t v) { return (v + 1) & ~int64_t(1); }
 
 // Group boundaries on the root dimension nr; each group gets a shared-memory layout sized for
 // its largest instance.
-static const int kBucketEdges[] = {32, 64, 96, 128, 160, 192, 256, 384, 512, 1024, 2048, 4096};
+// Roots above 128 rows run 256-thread CTAs, one per SM, so the 128-192 range is one bucket: one
+// history-ordered queue then starts all of its slowest instances first.
+static const int kBucketEdges[] = {32, 64, 96, 128, 192, 256, 384, 512, 1024, 2048, 4096};
 // Root sizes: the largest one-CTA root; cxg_solver spreads roots above kGridAutoRoot rows over
 // every SM (whole_gpu_root = 0), which accepts up to kGridMaxRoot rows (a 70 GB FP64 root).
 static const int kCtaMaxRoot = 4096;
@@ -605,9 +607,83 @@ static LaunchArgs solveArgs(const cxg_batch* B, const Group& g, const DevSetting
   return a;
 }
 
+// ------------------------------------------------------------------------------------------
+// history-ordered queues: after each solve, every size bucket's queue is re-sorted by the cost
+// its instances just had (iterations x nr^3, x4 when the instance held the double-float factor),
+// so that in a timestep loop the instances that ran longest start first next time. A bucket's
+// makespan is set by its slowest instances; started late, they would end the batch late.
+// The order only decides which CTA takes an instance and when: each instance's arithmetic, and
+// so every result bit, is the same in any order.
+// ------------------------------------------------------------------------------------------
+constexpr int kSortMax = 4096;  // buckets with more instances keep their set-up order
+constexpr int kMaxGroups = 16;
+struct GroupRanges {
+  int begin[kMaxGroups], count[kMaxGroups];
+};
+
+__global__ void __launch_bounds__(1024) reorderKernel(const InstanceDesc* desc, const DevResult* res, int* order,
+                                                      GroupRanges gr) {
+  __shared__ double key[kSortMax];
+  __shared__ int idx[kSortMax];
+  const int n = gr.count[blockIdx.x];
+  int* o = order + gr.begin[blockIdx.x];
+  if (n < 2 || n > kSortMax) return;
+  int N = 1;
+  while (N < n) N <<= 1;
+  for (int i = threadIdx.x; i < N; i += blockDim.x) {
+    if (i < n) {
+      const int inst = o[i];
+      const DevResult& r = res[inst];
+      const int it = r.iterations > 0 ? r.iterations : 1;
+      key[i] = desc[inst].cost * (double)it * (r.fp64_fallbacks > 0 ? 4.0 : 1.0);
+      idx[i] = inst;
+    } else {
+      key[i] = -1.0;  // padding sorts last
+      idx[i] = 0x7fffffff;
+    }
+  }
+  __syncthreads();
+  // bitonic sort, descending key, ties by ascending instance index (deterministic)
+  for (int k = 2; k <= N; k <<= 1) {
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      for (int i = threadIdx.x; i < N; i += blockDim.x) {
+        const int p = i ^ j;
+        if (p > i) {
+          const bool before = key[i] > key[p] || (key[i] == key[p] && idx[i] < idx[p]);  // i ahead of p
+          const bool desc_ = (i & k) == 0;
+          if (desc_ ? !before : before) {
+            const double tk = key[i];
+            key[i] = key[p];
+            key[p] = tk;
+            const int ti = idx[i];
+            idx[i] = idx[p];
+            idx[p] = ti;
+          }
+        }
+      }
+      __syncthreads();
+    }
+  }
+  for (int i = threadIdx.x; i < n; i += blockDim.x) o[i] = idx[i];
+}
+
+static int enqueueReorder(cxg_batch* B, cudaStream_t s) {
+  const int G = (int)B->groups.size();
+  if (G < 1 || G > kMaxGroups) return CXG_OK;
+  GroupRanges gr{};
+  for (int gi = 0; gi < G; ++gi) {
+    gr.begin[gi] = B->groups[(size_t)gi].begin;
+    gr.count[gi] = B->groups[(size_t)gi].count;
+  }
+  reorderKernel<<<G, 1024, 0, s>>>(B->dDesc, B->dRes, B->dOrder, gr);
+  CX_CUDA(cudaGetLastError());
+  return CXG_OK;
+}
+
 // Enqueues the device-side solve sequence on `s`: queue resets, then one persistent launch per
 // size bucket, each on its own stream forked from and joined back into `s`, so the buckets run
-// concurrently and the batch waits for its slowest instance once rather than once per bucket.
+// concurrently and the batch waits for its slowest instance once rather than once per bucket;
+// then the queues are re-ordered for the next solve (history-ordered queues, above).
 static int enqueueSolve(cxg_batch* B, cudaStream_t s) {
   const DevSettings ds = makeDevSettings(B->st, B->kktSt);
   CX_CUDA(cudaMemsetAsync(B->dCounters, 0, sizeof(int) * (B->groups.size() + 1), s));
@@ -652,7 +728,9 @@ static int enqueueSolve(cxg_batch* B, cudaStream_t s) {
       CX_CUDA(cudaStreamWaitEvent(s, B->forkJoin[gi + 1], 0));
     }
   }
-  B->lastLaunches = (int)G;
+  int rc = enqueueReorder(B, s);
+  if (rc) return rc;
+  B->lastLaunches = (int)G + ((G >= 1 && G <= (size_t)kMaxGroups) ? 1 : 0);  // bucket launches + reorder
   return CXG_OK;
 }
 
@@ -677,7 +755,8 @@ static int runSolve(cxg_batch* B, cudaStream_t s) {
     B->graphValid = true;
   }
   CX_CUDA(cudaGraphLaunch(B->graphExec, s));
-  B->lastLaunches = (int)B->groups.size();
+  const size_t G = B->groups.size();
+  B->lastLaunches = (int)G + ((G >= 1 && G <= (size_t)kMaxGroups) ? 1 : 0);
   return CXG_OK;
 }
 
