@@ -777,6 +777,34 @@ __device__ void tileSyrk(T* C, const T* A, const T* B, const T* Ajj) {
   }
 }
 
+// One 16x16 quadrant (qr, qc) of tileSyrk's C -= A diag(d) B^T, one warp: lane (r4, c2) takes
+// rows qr*16 + 4 r4 + {0..3} and columns qc*16 + 2 c2 + {0, 1}. Every entry gets tileSyrk's
+// operations in its order, so the result is the same.
+template <typename T>
+__device__ void tileSyrkQuad(T* C, const T* A, const T* B, const T* Ajj, int qr, int qc) {
+  const int lane = threadIdx.x & 31, r0 = qr * 16 + (lane & 3) * 4, c0 = qc * 16 + (lane >> 2) * 2;
+  T acc[4][2];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) acc[i][0] = acc[i][1] = (T)0;
+#pragma unroll 4
+  for (int k = 0; k < 32; ++k) {
+    const T dk = Ajj[k * kTileLd + k];
+    T av[4], bv[2];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) av[i] = A[k * kTileLd + r0 + i];
+#pragma unroll
+    for (int j = 0; j < 2; ++j) bv[j] = B[k * kTileLd + c0 + j] * dk;
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int j = 0; j < 2; ++j) acc[i][j] = accT(acc[i][j], av[i], bv[j]);
+  }
+#pragma unroll
+  for (int j = 0; j < 2; ++j)
+#pragma unroll
+    for (int i = 0; i < 4; ++i) C[(c0 + j) * kTileLd + r0 + i] -= accEnd(acc[i][j]);
+}
+
 template <typename T>
 __device__ __noinline__ void denseLdlt(Ctx& c, T* M, const DevSettings& st, int& fail, int& wrongSign, double& minAbsD) {
   const int nr = c.nr, nx = c.n, Tn = rootTiles(nr);
@@ -799,10 +827,18 @@ __device__ __noinline__ void denseLdlt(Ctx& c, T* M, const DevSettings& st, int&
     __syncthreads();
     const int rem = Tn - J - 1;
     const int npairs = rem * (rem + 1) / 2;
+    if (nw >= 4 && warp < 3) {
+      // the next diagonal tile's update, the head of the critical path, on three warps: the
+      // quadrants the factorisation reads (the upper-right one is overwritten by Linv anyway)
+      T* Anext = M + tileBase(Tn, J + 1, J + 1);
+      const T* Lnext = M + tileBase(Tn, J + 1, J);
+      tileSyrkQuad<T>(Anext, Lnext, Lnext, Ajj, warp == 0 ? 0 : 1, warp == 2 ? 1 : 0);
+      asm volatile("bar.sync 1, 96;" ::: "memory");
+    }
     if (warp == 0 || nw == 1) {
       T* Anext = M + tileBase(Tn, J + 1, J + 1);
       const T* Lnext = M + tileBase(Tn, J + 1, J);
-      tileSyrk<T>(Anext, Lnext, Lnext, Ajj);
+      if (nw < 4) tileSyrk<T>(Anext, Lnext, Lnext, Ajj);
       if (nw == 1) {
         for (int t = 1; t < npairs; ++t) {
           int K = J + 1, tt = t, len = rem;
