@@ -363,6 +363,21 @@ def test_autotune_keeps_results():
         assert np.max(np.abs(a - b)) <= 1e-5 * max(1.0, np.max(np.abs(b))), i
 
 
+def test_history_ordered_queues_keep_results():
+    """The bucket queues are re-ordered after every solve (the instances that ran longest go
+    first); each instance's arithmetic does not depend on its place in the queue, so repeated
+    solves of the same values give the same bits, iterations and statuses."""
+    _, BatchSolver = _solvers()
+    qps = generators.contact_batch(512, base_seed=9000)
+    B = BatchSolver(qps, warm_start=0)
+    x0, s0, z0, i0 = B.solve()
+    x1, s1, z1, i1 = B.solve()  # queue order now from the first solve's iteration counts
+    x2, s2, z2, i2 = B.solve()
+    for xa, sa, za, ia in ((x1, s1, z1, i1), (x2, s2, z2, i2)):
+        assert np.array_equal(ia["status"], i0["status"]) and np.array_equal(ia["iterations"], i0["iterations"])
+        assert np.array_equal(xa, x0) and np.array_equal(sa, s0) and np.array_equal(za, z0)
+
+
 @pytest.mark.parametrize("whole_gpu_root", [-1, 1])
 @pytest.mark.parametrize("precision", [_abi.PRECISION_FP64, _abi.PRECISION_MIXED])
 def test_larger_instance_root_in_scratch(oracle_mod, precision, whole_gpu_root):
