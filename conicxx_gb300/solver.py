@@ -45,7 +45,9 @@ def _settings(settings, default_precision, **kw):
 
 
 class Solver:
-    """Single-instance solver (FP64 factorisation by default: the plain per-instance GPU form)."""
+    """Single-instance solver (FP64 factorisation by default: the plain per-instance GPU form).
+    A root of more than 512 rows (n + zero_dim) is spread over every SM (whole_gpu_root setting:
+    0 automatic, 1 always, -1 never)."""
 
     def __init__(self):
         h = C.c_void_p()
