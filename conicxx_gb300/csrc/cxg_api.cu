@@ -151,6 +151,7 @@ struct cxg_batch {
   double setupTime = 0.0;
   int device = 0;
   bool gridMode = false;                    // one instance, root spread over every SM (launchIpmGrid)
+  bool bwdDropped = false;                  // differentiable asked for, not kept (whole-GPU root > 8192 rows)
   void* dGridCtl = nullptr;                 // its control block
 
   ~cxg_batch() {
@@ -446,13 +447,15 @@ extern "C" int cxg_batch_create(cxg_batch** out, int count, const cxg_problem* p
   const bool gridMode = count == 1 && (st.whole_gpu_root == 1 || nr0 > kCtaMaxRoot);
   // the adjoint keeps an FP64 copy of the final factor and solves with it on one CTA: offered up
   // to 8192 root rows
-  if (gridMode && nr0 > kGridMaxAdjointRoot) st.differentiable = 0;
+  const bool bwdDropped = gridMode && nr0 > kGridMaxAdjointRoot && st.differentiable;
+  if (bwdDropped) st.differentiable = 0;
   cxg_batch* B = new (std::nothrow) cxg_batch();
   if (!B) return setErr(CXG_E_NOMEM, "host allocation failed");
   B->count = count;
   B->st = st;
   B->kktSt = st;
   B->gridMode = gridMode;
+  B->bwdDropped = bwdDropped;
   try {
     // Host planning, the set-up cost when contact patterns change: contiguous chunks of instances
     // are planned on worker threads into their own pools, then appended in instance order.
@@ -1154,6 +1157,8 @@ static int enqueueAdjoint(cxg_batch* B, cudaStream_t s, const double* gx, double
 
 static int checkDifferentiable(cxg_batch* B) {
   if (!B) return setErr(CXG_E_INVALID, "null batch");
+  if (!B->dBwd && B->bwdDropped)
+    return setErr(CXG_E_UNSUPPORTED, "backward is offered up to 8192 root rows on the whole-GPU root");
   if (!B->dBwd) return setErr(CXG_E_NOT_SETUP, "backward needs settings.differentiable = 1 at set-up");
   if (B->forkJoin.empty()) return setErr(CXG_E_NOT_SETUP, "backward before any solve");
   return CXG_OK;
