@@ -47,6 +47,7 @@ SIGNATURES = {
     "cxg_batch_solve_device_noalloc": (C.c_int, [vp, vp, vp, vp, IP, vp]),
     "cxg_batch_autotune": (C.c_int, [vp, C.c_int, C.c_char_p, C.c_int]),
     "cxg_dense_ldlt": (C.c_int, [C.c_int, C.c_int, vp, vp, C.c_int, C.c_int, C.c_int, vp, vp, vp, vp, vp]),
+    "cxg_grid_barrier_selftest": (C.c_int, [C.c_int, C.c_int, C.c_double, vp, vp, vp]),
     "cxg_batch_backward": (C.c_int, [vp, dp, dp, dp, dp, dp]),
     "cxg_batch_backward_device": (C.c_int, [vp, vp, vp, vp, vp, vp, vp]),
     "cxg_batch_last_launches": (C.c_int, [vp]),

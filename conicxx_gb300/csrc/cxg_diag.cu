@@ -252,3 +252,19 @@ extern "C" int cxg_dense_ldlt(int nr, int nx, const double* K, const double* b, 
   for (void* p : bufs) cudaFree(p);
   return CXG_OK;
 }
+
+extern "C" int cxg_grid_barrier_selftest(int skip_cta, int rounds, double timeout_s, int* error_flag,
+                                         int* max_rounds_passed, double* elapsed_s) {
+  using namespace cxg;
+  if (rounds < 1 || rounds > 100000 || !(timeout_s >= 1e-3 && timeout_s <= 5.0) || !error_flag ||
+      !max_rounds_passed || !elapsed_s) {
+    lastErrorRef() = "cxg_grid_barrier_selftest: bad arguments";
+    return CXG_E_INVALID;
+  }
+  cudaError_t e = launchGridBarrierTest(skip_cta, rounds, timeout_s, error_flag, max_rounds_passed, elapsed_s);
+  if (e != cudaSuccess) {
+    lastErrorRef() = std::string("cxg_grid_barrier_selftest: ") + cudaGetErrorString(e);
+    return CXG_E_CUDA;
+  }
+  return CXG_OK;
+}

@@ -995,6 +995,7 @@ struct GridCtl {
   void* y;           // solve vector (root arithmetic), rootTiles(nr) * 32 entries
   double ep, ea;     // regularisation bumps of the assembly
   int64_t stageOff;  // byte offset of the tile staging area in dynamic shared memory
+  unsigned long long waitNs;  // longest barrier wait; 0 = kGridWaitNs
   Ctx ctx;           // CTA 0's instance context (pointers into global memory only)
 };
 
@@ -1032,6 +1033,8 @@ static __device__ __noinline__ bool gridSync(GridCtl* g) {
     volatile GridCtl* vg = g;
     int ok = vg->error == 0;
     if (ok) {
+      unsigned long long limit = vg->waitNs;
+      if (limit == 0) limit = kGridWaitNs;
       const unsigned gen = vg->gen;
       __threadfence();
       const unsigned prev = atomicAdd(&g->arrive, 1u);
@@ -1044,7 +1047,7 @@ static __device__ __noinline__ bool gridSync(GridCtl* g) {
         unsigned backoff = 32;  // ns, doubled up to 512 while the wait lasts
         while (vg->gen == gen) {
           if (vg->error) { ok = 0; break; }
-          if (globalNs() - t0 > kGridWaitNs) {
+          if (globalNs() - t0 > limit) {
             atomicExch(&g->error, 1);
             ok = 0;
             break;

@@ -1,5 +1,9 @@
 // Diagnostic entry of the dense root (cxg_dense_ldlt): the root LDL' and triangular solves of
 // the interior-point kernels (cxg_ipm.cuh) on one given matrix, on one CTA or on the whole GPU.
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
 #include "cxg_ipm.cuh"
 
 // ------------------------------------------------------------------------------------------
@@ -147,6 +151,78 @@ static cudaError_t probeGridLaunch(int nr, int nx, const double* K, const double
   if (M) cudaFree(M);
   if (y) cudaFree(y);
   if (g) cudaFree(g);
+  return e;
+}
+
+// Barrier time-out self-test: every CTA passes `rounds` grid barriers, except CTA `skip` (when
+// >= 0), which returns at once. The others' first wait then runs out after ctl->waitNs, the error
+// flag is set and every barrier fails, so the launch ends without that CTA. passed[b] = barriers
+// CTA b got through (-1 for the skipping CTA).
+__global__ void __launch_bounds__(256) gridBarrierTestKernel(GridCtl* g, int skip, int rounds, int* passed) {
+  if ((int)blockIdx.x == skip) {
+    if (threadIdx.x == 0) passed[blockIdx.x] = -1;
+    return;
+  }
+  int n = 0;
+  for (int r = 0; r < rounds; ++r) {
+    if (!gridSync(g)) break;
+    ++n;
+  }
+  if (threadIdx.x == 0) passed[blockIdx.x] = n;
+}
+
+cudaError_t launchGridBarrierTest(int skip, int rounds, double timeoutS, int* errorFlag, int* maxPassed,
+                                  double* elapsedS) {
+  int dev = 0, numSM = 0, occ = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&numSM, cudaDevAttrMultiProcessorCount, dev);
+  if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, gridBarrierTestKernel, 256, 0);
+  if (e != cudaSuccess) return e;
+  if (occ < 1 || numSM < 2) return cudaErrorInvalidConfiguration;
+  const int grid = numSM;  // one CTA per SM, all resident
+  GridCtl* g = nullptr;
+  int* passed = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  e = cudaMalloc((void**)&g, sizeof(GridCtl));
+  if (e == cudaSuccess) e = cudaMalloc((void**)&passed, sizeof(int) * grid);
+  if (e == cudaSuccess) e = cudaEventCreate(&e0);
+  if (e == cudaSuccess) e = cudaEventCreate(&e1);
+  if (e == cudaSuccess) {
+    GridCtl h;
+    std::memset(&h, 0, sizeof(h));
+    h.waitNs = (unsigned long long)(timeoutS * 1e9);
+    e = cudaMemcpy(g, &h, sizeof(h), cudaMemcpyHostToDevice);
+  }
+  if (e == cudaSuccess) {
+    int sk = skip, rd = rounds;
+    void* args[] = {(void*)&g, &sk, &rd, (void*)&passed};
+    e = cudaEventRecord(e0, nullptr);
+    if (e == cudaSuccess)
+      e = cudaLaunchCooperativeKernel((const void*)gridBarrierTestKernel, dim3(grid), dim3(256), args, 0, nullptr);
+    if (e == cudaSuccess) e = cudaEventRecord(e1, nullptr);
+    if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+  }
+  if (e == cudaSuccess) {
+    float ms = 0.0f;
+    e = cudaEventElapsedTime(&ms, e0, e1);
+    *elapsedS = 1e-3 * ms;
+  }
+  if (e == cudaSuccess) {
+    GridCtl h;
+    std::vector<int> p((size_t)grid);
+    e = cudaMemcpy(&h, g, sizeof(h), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(p.data(), passed, sizeof(int) * grid, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) {
+      *errorFlag = h.error;
+      int mx = -1;
+      for (int v : p) mx = std::max(mx, v);
+      *maxPassed = mx;
+    }
+  }
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  if (g) cudaFree(g);
+  if (passed) cudaFree(passed);
   return e;
 }
 

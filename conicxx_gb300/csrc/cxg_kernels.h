@@ -78,6 +78,10 @@ cudaError_t ipmOccupancy(int* blocksPerSM, int block, size_t smem, bool fp32);
 // arithmetic (0 FP64, 1 FP32, 2 double-float) on one CTA of `threads` threads, then solve K x = b.
 // Outputs L (unit lower, column-major), D, x, cycles {ldlt, solve}, flags {fail, wrong sign}.
 size_t denseProbeSmem(int arith, int nr);
+// Diagnostic: the whole-GPU grid barrier with one CTA (skip >= 0) never arriving; the wait limit
+// is timeoutS. Reports the error flag, the most barriers any CTA passed and the launch time.
+cudaError_t launchGridBarrierTest(int skip, int rounds, double timeoutS, int* errorFlag, int* maxPassed,
+                                  double* elapsedS);
 cudaError_t launchDenseProbe(int arith, int nr, int nx, const double* K, const double* b, const DevSettings& st,
                              int threads, double* L, double* D, double* x, long long* cyc, int* flags);
 

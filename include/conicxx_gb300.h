@@ -278,6 +278,15 @@ int cxg_cones_eval(int op, int zero_dim, int nonneg_dim, int n_soc, const int* s
  * out. */
 int cxg_dense_ldlt(int nr, int nx, const double* K, const double* b, int arith, int threads, int linear_solver,
                    double* L, double* D, double* x, long long* cycles, int* flags);
+
+/* Diagnostic, no reference counterpart: the bounded wait of the whole-GPU root's grid barrier.
+ * One cooperative launch of one CTA per SM passes `rounds` grid barriers; when skip_cta >= 0 that
+ * CTA returns without arriving, so the others' first wait runs out after timeout_s (1e-3..5 s),
+ * the barrier's error flag is set and every CTA returns (a large instance whose barrier runs out
+ * ends with NumericalError and error_code 1 the same way). Outputs: error_flag (1 when a wait ran
+ * out), max_rounds_passed (most barriers any CTA got through), elapsed_s (launch time). */
+int cxg_grid_barrier_selftest(int skip_cta, int rounds, double timeout_s, int* error_flag, int* max_rounds_passed,
+                              double* elapsed_s);
 /* Host equilibration of the set-up path (Equilibration::compute, src/conicxx/kkt/equilibration.cpp:8-100):
  * d (n), e (m), c. No GPU needed. */
 int cxg_equilibration(const cxg_problem* problem, const cxg_settings* settings, double* d, double* e, double* c);

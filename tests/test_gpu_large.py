@@ -207,3 +207,22 @@ def test_large_sparse_qp_full_size_mixed():
     if sol.status == _abi.STATUS_SOLVED:
         st, fe, sz = qp.kkt_residuals(sol.x, sol.s, sol.z)
         assert fe < 1e-5 and sz < 1e-5
+
+
+def test_grid_barrier_wait_runs_out_and_reports():
+    """The whole-GPU root's barrier wait is bounded. With one CTA that never arrives, the others'
+    first wait runs out after the limit (0.2 s here), the error flag is set and every CTA returns;
+    the context stays usable. With every CTA arriving, all barriers are passed."""
+    import ctypes as C
+
+    L = _lib.lib()
+    err, mx, el = C.c_int(), C.c_int(), C.c_double()
+    assert L.cxg_grid_barrier_selftest(1, 3, 0.2, C.byref(err), C.byref(mx), C.byref(el)) == _abi.OK
+    assert err.value == 1 and mx.value == 0 and 0.15 < el.value < 5.0, (err.value, mx.value, el.value)
+    # the device is still usable: a whole-GPU factorisation right after
+    K = _quasi_definite(64, 48, 3)
+    b = np.ones(64)
+    _, _, x, f = _probe(K, 48, b, "fp64", -1)
+    assert f[2] == 0 and rel(x, np.linalg.solve(K, b)) < 1e-10
+    assert L.cxg_grid_barrier_selftest(-1, 200, 0.2, C.byref(err), C.byref(mx), C.byref(el)) == _abi.OK
+    assert err.value == 0 and mx.value == 200, (err.value, mx.value)
