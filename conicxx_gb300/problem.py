@@ -135,6 +135,31 @@ class QP:
     def m(self):
         return int(self.zero + self.nonneg + sum(self.soc))
 
+    @staticmethod
+    def from_dense(P, q, A, b, zero=0, nonneg=0, soc=(), name=""):
+        """QP from dense (numpy) or Csc inputs: the dense-input Solver::setup overloads
+        (src/conicxx/solver.cpp:17-30). A dense P becomes its upper triangle with every entry kept
+        explicit (toSparseUpperTriangular, convert.cpp:43-70), a dense A every entry explicit
+        (toSparse, convert.cpp:22-41), so the pattern stays the same across conversions of new
+        values; an asymmetric dense P gets the reference's warning (only its upper triangle is
+        read)."""
+        if not isinstance(P, Csc):
+            Pd = np.asarray(P, dtype=np.float64)
+            if Pd.ndim == 2 and Pd.shape[0] == Pd.shape[1] and Pd.size:
+                asym = np.max(np.abs(Pd - Pd.T))
+                if asym > 1e-8 * max(1.0, np.max(np.abs(Pd))):
+                    import warnings
+
+                    warnings.warn("matrix passed as P is not numerically symmetric: only its upper "
+                                  "triangle is read", stacklevel=2)
+            P = Csc.from_dense(Pd, keep_zeros=True, upper=True)
+        if not isinstance(A, Csc):
+            A = Csc.from_dense(np.asarray(A, dtype=np.float64), keep_zeros=True)
+        qp = QP(P=P, q=np.asarray(q, dtype=np.float64), A=A, b=np.asarray(b, dtype=np.float64), zero=int(zero),
+                nonneg=int(nonneg), soc=[int(d) for d in soc], name=name)
+        qp.validate()
+        return qp
+
     def validate(self):
         assert self.P.shape == (self.n, self.n)
         assert self.A.shape == (self.m, self.n), (self.A.shape, self.m, self.n)

@@ -75,6 +75,11 @@ class Solver:
         self._solution = Solution()
         return True
 
+    def setup_dense(self, P, q, A, b, zero=0, nonneg=0, soc=(), settings: Settings = None, **kw) -> bool:
+        """The dense-input setup overloads (src/conicxx/solver.cpp:17-30): P and/or A as numpy
+        arrays (or Csc), converted as the reference converts them (QP.from_dense)."""
+        return self.setup(QP.from_dense(P, q, A, b, zero, nonneg, soc), settings, **kw)
+
     def update_data(self, P: Csc = None, q=None, A: Csc = None, b=None) -> bool:
         keep = []
 

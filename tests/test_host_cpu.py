@@ -172,6 +172,26 @@ def test_whole_gpu_setting_rejections():
     assert _lib.lib().cxg_batch_create(C.byref(h), 2, arr, C.byref(st)) == _abi.E_UNSUPPORTED
 
 
+def test_dense_inputs_convert_like_the_reference():
+    """QP.from_dense (the dense-input setup overloads): P's upper triangle and all of A with every
+    entry explicit, the same products as the sparse problem, and the reference's warning for an
+    asymmetric P."""
+    import warnings
+
+    P = np.eye(3)
+    A = np.array([[1.0, 1, 0], [0, 0, -1], [0, 0, -1], [-1, 0, 0], [0, -1, 0]])
+    q, b = np.array([-1.0, -1, -0.3]), np.array([1.0, 0, 0, 0, 0])
+    qp = QP.from_dense(P, q, A, b, zero=1, nonneg=1, soc=[3])
+    assert qp.P.nnz == 6 and qp.A.nnz == 15  # upper triangle of 3x3, all 5x3 entries
+    assert np.all(qp.P.indices <= qp.P.col_of_entries())
+    x = np.array([0.3, -0.7, 1.1])
+    assert np.allclose(sym_upper_matvec(qp.P, x), P @ x) and np.allclose(qp.A.matvec(x), A @ x)
+    with warnings.catch_warnings(record=True) as w:
+        warnings.simplefilter("always")
+        QP.from_dense(np.array([[1.0, 2.0], [0.0, 1.0]]), np.zeros(2), np.eye(2), np.ones(2), nonneg=2)
+    assert any("symmetric" in str(x_.message) for x_ in w)
+
+
 def test_sharding_balanced():
     qps = generators.contact_batch(64)
     costs = [instance_cost(q) for q in qps]
