@@ -363,6 +363,20 @@ def test_autotune_keeps_results():
         assert np.max(np.abs(a - b)) <= 1e-5 * max(1.0, np.max(np.abs(b))), i
 
 
+def test_dense_input_setup_solves_readme_example():
+    """The README example through the dense-input setup (P and A as numpy arrays, every entry
+    explicit as the reference's toSparse keeps them): x = (0.5, 0.5, sqrt(0.5))."""
+    from conicxx_gb300 import Solver
+
+    S = Solver()
+    A = np.array([[1.0, 1, 0], [0, 0, -1], [0, 0, -1], [-1, 0, 0], [0, -1, 0]])
+    assert S.setup_dense(np.eye(3), np.array([-1.0, -1, -0.3]), A, np.array([1.0, 0, 0, 0, 0]), zero=1, nonneg=1,
+                         soc=[3])
+    sol = S.solve()
+    assert sol.ok(), sol.status_name
+    assert np.allclose(sol.x, [0.5, 0.5, np.sqrt(0.5)], atol=1e-6), sol.x
+
+
 def test_history_ordered_queues_keep_results():
     """The bucket queues are re-ordered after every solve (the instances that ran longest go
     first); each instance's arithmetic does not depend on its place in the queue, so repeated
