@@ -1,15 +1,18 @@
-// The interior-point hot path on the GPU (device code; instantiated by cxg_ipm_f32.cu,
-// cxg_ipm_f64.cu and cxg_ipm_probe.cu, which compile in parallel): one CTA runs the complete homogeneous self-dual
-// embedding IPM of ConicXX (src/conicxx/solver_impl.cpp:220-560 as numbered in that file's
-// SolverImpl::solve and helpers) for one instance at a time, taking instances from an atomic
-// work queue (persistent CTAs, heaviest instances first). All iterates live in shared memory;
-// the problem data is read from HBM/L2.
+// The interior-point hot path on the GPU (device code, instantiated by cxg_ipm_f32.cu,
+// cxg_ipm_f32s.cu, cxg_ipm_f64.cu, cxg_ipm_gridf.cu, cxg_ipm_gridd.cu and cxg_ipm_probe.cu, which
+// compile in parallel). One CTA runs the complete homogeneous self-dual embedding IPM of ConicXX
+// (SolverImpl::solve and its helpers, src/conicxx/solver_impl.cpp:102-466) for one instance:
+//  - batched form (ipmKernel): persistent CTAs take instances from an atomic queue per size
+//    bucket; iterates in shared memory when they fit, the problem data in HBM/L2;
+//  - whole-GPU form (ipmGridKernel): one large instance, CTA 0 running the iteration on vectors in
+//    its scratch while every SM joins the root assembly, LDL' and triangular solves (gridSync).
 //
 // Precision: cone scaling, residuals, refinement residuals, step lengths and termination are
 // FP64. The dense root LDL' (see cxg_layout.h) is FP32 (MIXED) or FP64. In MIXED mode a KKT
 // solve whose FP64-refined relative residual stays above mixed_fallback_tol (or is not finite),
-// or whose FP32 factor has a pivot of the wrong sign, switches that instance to an FP64 factor
-// for the rest of its solve ("sticky" fallback; counted in DevResult::fp64_fallbacks).
+// or whose FP32 factor has a pivot of the wrong sign, switches that instance to the double-float
+// factor (about 48 bits, on the FP32 pipe) for the rest of its solve ("sticky" fallback, counted
+// in DevResult::fp64_fallbacks).
 #pragma once
 
 #include <cuda_runtime.h>
