@@ -209,10 +209,12 @@ static int64_t r2(int64_t v) { return (v + 1) & ~int64_t(1); }
 // history-ordered queue then starts all of its slowest instances first.
 static const int kBucketEdges[] = {32, 64, 96, 128, 192, 256, 384, 512, 1024, 2048, 4096};
 // Root sizes: the largest one-CTA root; cxg_solver spreads roots above kGridAutoRoot rows over
-// every SM (whole_gpu_root = 0), which accepts up to kGridMaxRoot rows (a 70 GB FP64 root).
+// every SM (whole_gpu_root = 0), which accepts up to kGridMaxRoot rows: the root's element
+// offsets must fit the 32-bit root index maps of the plan (rootSize(64512) = 2.147e9 < 2^31; a
+// 68000-row root, 2.39e9 elements, would wrap them).
 static const int kCtaMaxRoot = 4096;
 static const int kGridAutoRoot = 512;
-static const int kGridMaxRoot = 131072;
+static const int kGridMaxRoot = 64512;
 static const int kGridMaxAdjointRoot = 8192;
 // shared memory of the whole-GPU trailing update (8-byte entries; see gridStageBytes)
 static const int64_t kGridStageBytes = (2ll * kTile * 128 + 16ll * kTileElems) * 8;
@@ -439,7 +441,7 @@ extern "C" int cxg_batch_create(cxg_batch** out, int count, const cxg_problem* p
       return setErr(CXG_E_UNSUPPORTED,
                     "instance " + std::to_string(i) + ": n + zero_dim = " + std::to_string(nr) +
                         " exceeds the one-CTA root (4096 rows); a single instance (count 1, whole_gpu_root >= 0) "
-                        "takes the whole-GPU root up to 131072 rows");
+                        "takes the whole-GPU root up to 64512 rows");
   }
   // One instance whose root one CTA cannot hold, or when asked: spread the root over every SM.
   // (cxg_solver_setup asks for it from kGridAutoRoot rows on.)

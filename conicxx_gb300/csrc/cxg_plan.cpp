@@ -4,6 +4,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
+#include <stdexcept>
 #include <utility>
 
 namespace cxg {
@@ -118,6 +119,8 @@ void planInstance(const cxg_problem& pr, const cxg_settings& st, Pools& pools) {
   InstanceDesc D{};
   const int n = pr.n, m = pr.m, p = pr.zero_dim, l = pr.nonneg_dim, nsoc = pr.n_soc;
   const int nr = n + p;
+  // the root scatter maps below hold element offsets of the root in 32-bit ints
+  if (rootSize(nr) > (int64_t)INT32_MAX) throw std::runtime_error("root too large for 32-bit root index maps");
   D.n = n; D.m = m; D.p = p; D.l = l; D.nsoc = nsoc; D.nr = nr;
   D.nnzPu = pr.Pp[n];
   D.nnzA = pr.Ap[n];

@@ -97,7 +97,7 @@ typedef struct cxg_settings {
                                  device so backward() can reuse them (default 0; cxg_solver: 1);
                                  ignored for whole-GPU roots above 8192 rows */
   int whole_gpu_root;         /* one instance (cxg_solver, or a batch of count 1): 1 = spread the root
-                                 over every SM (cooperative launch, roots up to 131072 rows); -1 =
+                                 over every SM (cooperative launch, roots up to 64512 rows); -1 =
                                  never (one CTA, roots up to 4096 rows); 0 = automatic: cxg_solver
                                  spreads roots of more than 512 rows, a batch of one only roots of
                                  more than 4096 */

@@ -170,6 +170,16 @@ def test_whole_gpu_setting_rejections():
     arr = (_abi.Problem * 2)(prob, prob)
     st = _abi.default_settings()
     assert _lib.lib().cxg_batch_create(C.byref(h), 2, arr, C.byref(st)) == _abi.E_UNSUPPORTED
+    # the whole-GPU root's limit: element offsets of the root must fit the 32-bit scatter maps
+    # (64512 rows: 2.147e9 elements; 64513 rows needs a 2017th tile column, 2.149e9 > 2^31 - 1)
+    n = 64513
+    P = Csc.from_coo(n, n, np.arange(n), np.arange(n), np.ones(n))
+    A = Csc.from_coo(1, n, [0], [0], [-1.0])
+    big = QP(P, np.zeros(n), A, np.ones(1), 0, 1, [])
+    prob, keep = make_problem_struct(big)
+    st = _abi.default_settings(whole_gpu_root=1)
+    assert _lib.lib().cxg_batch_create(C.byref(h), 1, C.byref(prob), C.byref(st)) == _abi.E_UNSUPPORTED
+    assert b"64512" in _lib.lib().cxg_last_error()
 
 
 def test_dense_inputs_convert_like_the_reference():
