@@ -55,6 +55,7 @@ SIGNATURES = {
     "cxg_batch_footprint": (C.c_int, [vp, i64p, i64p, i64p]),
     "cxg_cones_eval": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, ip, dp, dp, dp, dp, C.c_double, dp, dp, dp]),
     "cxg_equilibration": (C.c_int, [PP, SP, dp, dp, dp]),
+    "cxg_plan_inspect": (C.c_int, [PP, SP, i64p, i64p, i64p, i64p, C.c_int]),
 }
 
 

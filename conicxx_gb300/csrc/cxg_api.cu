@@ -209,12 +209,12 @@ static int64_t r2(int64_t v) { return (v + 1) & ~int64_t(1); }
 // history-ordered queue then starts all of its slowest instances first.
 static const int kBucketEdges[] = {32, 64, 96, 128, 192, 256, 384, 512, 1024, 2048, 4096};
 // Root sizes: the largest one-CTA root; cxg_solver spreads roots above kGridAutoRoot rows over
-// every SM (whole_gpu_root = 0), which accepts up to kGridMaxRoot rows: the root's element
-// offsets must fit the 32-bit root index maps of the plan (rootSize(64512) = 2.147e9 < 2^31; a
-// 68000-row root, 2.39e9 elements, would wrap them).
+// every SM (whole_gpu_root = 0), which accepts up to kGridMaxRoot rows. The plan's root scatter
+// maps hold 64-bit element offsets; a 131072-row root is 8.86e9 entries (71 GB of 8-byte
+// entries), and the host planner and tile indices stay within 32 bits up to there.
 static const int kCtaMaxRoot = 4096;
 static const int kGridAutoRoot = 512;
-static const int kGridMaxRoot = 64512;
+static const int kGridMaxRoot = 131072;
 static const int kGridMaxAdjointRoot = 8192;
 // shared memory of the whole-GPU trailing update (8-byte entries; see gridStageBytes)
 static const int64_t kGridStageBytes = (2ll * kTile * 128 + 16ll * kTileElems) * 8;
@@ -430,6 +430,8 @@ extern "C" int cxg_batch_create(cxg_batch** out, int count, const cxg_problem* p
   for (int i = 0; i < count; ++i) {
     std::string e = validateProblem(problems[i]);
     if (!e.empty()) return setErr(CXG_E_INVALID, "instance " + std::to_string(i) + ": " + e);
+    e = checkPlanCounts(problems[i]);
+    if (!e.empty()) return setErr(CXG_E_UNSUPPORTED, "instance " + std::to_string(i) + ": " + e);
     const cxg_problem& pr = problems[i];
     e = checkFinite(pr.Px, pr.Pp[pr.n], "P");
     if (e.empty()) e = checkFinite(pr.Ax, pr.Ap[pr.n], "A");
@@ -441,7 +443,7 @@ extern "C" int cxg_batch_create(cxg_batch** out, int count, const cxg_problem* p
       return setErr(CXG_E_UNSUPPORTED,
                     "instance " + std::to_string(i) + ": n + zero_dim = " + std::to_string(nr) +
                         " exceeds the one-CTA root (4096 rows); a single instance (count 1, whole_gpu_root >= 0) "
-                        "takes the whole-GPU root up to 64512 rows");
+                        "takes the whole-GPU root up to " + std::to_string(kGridMaxRoot) + " rows");
   }
   // One instance whose root one CTA cannot hold, or when asked: spread the root over every SM.
   // (cxg_solver_setup asks for it from kGridAutoRoot rows on.)
@@ -465,10 +467,14 @@ extern "C" int cxg_batch_create(cxg_batch** out, int count, const cxg_problem* p
     const int nth = std::max(1, std::min({hw, 32, count / 16}));
     std::vector<Pools> part((size_t)nth);
     std::vector<std::string> fail((size_t)nth);
+    std::vector<char> failLimit((size_t)nth, 0);
     auto work = [&](int t) {
       const int lo = (int)((int64_t)count * t / nth), hi = (int)((int64_t)count * (t + 1) / nth);
       try {
         for (int i = lo; i < hi; ++i) planInstance(problems[i], st, part[(size_t)t]);
+      } catch (const LimitError& ex) {
+        fail[(size_t)t] = ex.what();
+        failLimit[(size_t)t] = 1;
       } catch (const std::exception& ex) {
         fail[(size_t)t] = ex.what();
       }
@@ -482,7 +488,10 @@ extern "C" int cxg_batch_create(cxg_batch** out, int count, const cxg_problem* p
       for (std::thread& th : pool) th.join();
     }
     for (int t = 0; t < nth; ++t)
-      if (!fail[(size_t)t].empty()) throw std::runtime_error(fail[(size_t)t]);
+      if (!fail[(size_t)t].empty()) {
+        if (failLimit[(size_t)t]) throw LimitError(fail[(size_t)t]);
+        throw std::runtime_error(fail[(size_t)t]);
+      }
     for (const Pools& pp : part) appendPools(B->pools, pp);
     for (int i = 0; i < count; ++i) {
       const cxg_problem& pr = problems[i];
@@ -491,6 +500,9 @@ extern "C" int cxg_batch_create(cxg_batch** out, int count, const cxg_problem* p
       B->Ap.emplace_back(pr.Ap, pr.Ap + pr.n + 1);
       B->Ai.emplace_back(pr.Ai, pr.Ai + pr.Ap[pr.n]);
     }
+  } catch (const LimitError& ex) {
+    delete B;
+    return setErr(CXG_E_UNSUPPORTED, std::string("planning refused: ") + ex.what());
   } catch (const std::exception& ex) {
     delete B;
     return setErr(CXG_E_NOMEM, std::string("planning failed: ") + ex.what());

@@ -268,3 +268,51 @@ extern "C" int cxg_grid_barrier_selftest(int skip_cta, int rounds, double timeou
   }
   return CXG_OK;
 }
+
+extern "C" int cxg_plan_inspect(const cxg_problem* pr, const cxg_settings* st, long long* counts, long long* plow,
+                                long long* az, long long* tgt, int cap) {
+  if (!pr || !st || !counts) {
+    lastErrorRef() = "cxg_plan_inspect: null argument";
+    return CXG_E_INVALID;
+  }
+  std::string err = validateProblem(*pr);
+  if (!err.empty()) {
+    lastErrorRef() = err;
+    return CXG_E_INVALID;
+  }
+  err = checkPlanCounts(*pr);
+  if (!err.empty()) {
+    lastErrorRef() = err;
+    return CXG_E_UNSUPPORTED;
+  }
+  Pools pools;
+  pools.ipool.push_back(0);  // an odd start: the plan must re-align its 64-bit maps
+  try {
+    planInstance(*pr, *st, pools);
+  } catch (const LimitError& ex) {
+    lastErrorRef() = ex.what();
+    return CXG_E_UNSUPPORTED;
+  } catch (const std::exception& ex) {
+    lastErrorRef() = ex.what();
+    return CXG_E_NOMEM;
+  }
+  const InstanceDesc& D = pools.desc[0];
+  counts[0] = D.nr;
+  counts[1] = rootSize(D.nr);
+  counts[2] = D.nPlow;
+  counts[3] = D.nAZ;
+  counts[4] = D.nTgt;
+  counts[5] = D.nnzPs;
+  counts[6] = D.nAd;
+  counts[7] = D.nContrib;
+  counts[8] = ((D.iPlowIdx | D.iAZIdx | D.iTgtIdx) & 1) == 0 ? 1 : 0;
+  auto copy = [&](long long* out, int64_t off, int len) {
+    if (!out) return;
+    const int k = len < cap ? len : cap;
+    if (k > 0) std::memcpy(out, pools.ipool.data() + off, sizeof(long long) * (size_t)k);
+  };
+  copy(plow, D.iPlowIdx, D.nPlow);
+  copy(az, D.iAZIdx, D.nAZ);
+  copy(tgt, D.iTgtIdx, D.nTgt);
+  return CXG_OK;
+}

@@ -122,8 +122,9 @@ struct GridCtl;
 struct Ctx {
   int n, m, p, l, nsoc, nr, nUnits;
   const InstanceDesc* D;
-  const int *psRow, *psCol, *pdiag, *plowIdx, *plowSrc, *ap, *ai, *arRow, *arCol, *arSrc;
-  const int *azIdx, *azSrc, *socOff, *socDim, *unitAd, *unitSup, *tgtIdx, *tgtBeg, *contrib;
+  const int *psRow, *psCol, *pdiag, *plowSrc, *ap, *ai, *arRow, *arCol, *arSrc;
+  const int *azSrc, *socOff, *socDim, *unitAd, *unitSup, *tgtBeg, *contrib;
+  const long long *plowIdx, *azIdx, *tgtIdx;  // 64-bit root element offsets (8-byte aligned in the pool)
   // FP64 scratch (scaled data)
   double *Pu, *Pv, *Av, *Ad, *T, *qs, *bs, *root64;
   // shared-memory (or scratch) vectors
@@ -2161,13 +2162,13 @@ static __device__ void setupCtx(Ctx& c, const LaunchArgs& a, int inst, unsigned 
   c.n = D.n; c.m = D.m; c.p = D.p; c.l = D.l; c.nsoc = D.nsoc; c.nr = D.nr; c.nUnits = D.nUnits;
   const int* I = a.ipool;
   c.psRow = I + D.iPsRow; c.psCol = I + D.iPsCol; c.pdiag = I + D.iPdiag;
-  c.plowIdx = I + D.iPlowIdx; c.plowSrc = I + D.iPlowSrc;
+  c.plowIdx = reinterpret_cast<const long long*>(I + D.iPlowIdx); c.plowSrc = I + D.iPlowSrc;
   c.ap = I + D.iAp; c.ai = I + D.iAi;
   c.arRow = I + D.iArRow; c.arCol = I + D.iArCol; c.arSrc = I + D.iArSrc;
-  c.azIdx = I + D.iAZIdx; c.azSrc = I + D.iAZSrc;
+  c.azIdx = reinterpret_cast<const long long*>(I + D.iAZIdx); c.azSrc = I + D.iAZSrc;
   c.socOff = I + D.iSocOff; c.socDim = I + D.iSocDim;
   c.unitAd = I + D.iUnitAd; c.unitSup = I + D.iUnitSup;
-  c.tgtIdx = I + D.iTgtIdx; c.tgtBeg = I + D.iTgtBeg; c.contrib = I + D.iContrib;
+  c.tgtIdx = reinterpret_cast<const long long*>(I + D.iTgtIdx); c.tgtBeg = I + D.iTgtBeg; c.contrib = I + D.iContrib;
   // scratch carve-up for this instance (scaled P in user order, then its CSR-order copy)
   c.Pu = scratch + D.sPv;
   c.Pv = c.Pu + D.nnzPu;

@@ -4,6 +4,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
+#include <cstring>
 #include <stdexcept>
 #include <utility>
 
@@ -109,9 +110,64 @@ bool samePattern(const std::vector<int>& p_ref, const std::vector<int>& i_ref, i
   return nz == 0 || std::equal(i, i + nz, i_ref.begin());
 }
 
+std::string checkPlanCounts(const cxg_problem& pr) {
+  const int n = pr.n, m = pr.m, p = pr.zero_dim, l = pr.nonneg_dim;
+  int64_t upperOff = 0, diag = 0;
+  for (int c = 0; c < n; ++c)
+    for (int k = pr.Pp[c]; k < pr.Pp[c + 1]; ++k) {
+      if (pr.Pi[k] < c) ++upperOff;
+      else if (pr.Pi[k] == c) ++diag;
+    }
+  const int64_t nnzPs = 2 * upperOff + diag;
+  // A's rows: count entries per row, then each unit's distinct columns with a stamp per column
+  std::vector<int> rowStart((size_t)m + 1, 0);
+  for (int k = 0; k < pr.Ap[n]; ++k) rowStart[(size_t)pr.Ai[k] + 1]++;
+  for (int r = 0; r < m; ++r) rowStart[(size_t)r + 1] += rowStart[(size_t)r];
+  std::vector<int> rowCols((size_t)pr.Ap[n]);
+  {
+    std::vector<int> fill(rowStart.begin(), rowStart.end() - 1);
+    for (int c = 0; c < n; ++c)
+      for (int k = pr.Ap[c]; k < pr.Ap[c + 1]; ++k) rowCols[(size_t)fill[(size_t)pr.Ai[k]]++] = c;
+  }
+  std::vector<int> stamp((size_t)n, -1);
+  int64_t nAd = 0, nContrib = 0;
+  int r0 = p + l;
+  const int nUnits = l + pr.n_soc;
+  for (int u = 0; u < nUnits; ++u) {
+    const int lo = (u < l) ? p + u : r0;
+    const int d = (u < l) ? 1 : pr.soc_dims[u - l];
+    if (u >= l) r0 += d;
+    int64_t s = 0;
+    for (int r = lo; r < lo + d; ++r)
+      for (int k = rowStart[(size_t)r]; k < rowStart[(size_t)r + 1]; ++k)
+        if (stamp[(size_t)rowCols[(size_t)k]] != u) { stamp[(size_t)rowCols[(size_t)k]] = u; ++s; }
+    nAd += (int64_t)d * s;
+    nContrib += s * (s + 1) / 2;
+  }
+  if (nnzPs > INT32_MAX)
+    return "the full symmetric P has " + std::to_string(nnzPs) + " entries, above the plan's 32-bit limit " +
+           std::to_string(INT32_MAX);
+  if (nAd > INT32_MAX)
+    return "the densified cone-unit A blocks hold " + std::to_string(nAd) + " entries, above the plan's 32-bit limit";
+  if (3 * nContrib > INT32_MAX)
+    return "the cone units make " + std::to_string(nContrib) + " root contributions, above the plan's limit " +
+           std::to_string(INT32_MAX / 3);
+  return "";
+}
+
 static int64_t pushInts(std::vector<int>& pool, const std::vector<int>& v) {
   const int64_t off = (int64_t)pool.size();
   pool.insert(pool.end(), v.begin(), v.end());
+  return off;
+}
+
+// 64-bit root element offsets, stored in the int pool as two ints each at an 8-byte-aligned pool
+// offset (the pool is padded to an even length first; appendPools keeps the parity).
+static int64_t pushOffsets(std::vector<int>& pool, const std::vector<int64_t>& v) {
+  if (pool.size() & 1) pool.push_back(0);
+  const int64_t off = (int64_t)pool.size();
+  pool.resize(pool.size() + 2 * v.size());
+  if (!v.empty()) std::memcpy(pool.data() + off, v.data(), v.size() * sizeof(int64_t));
   return off;
 }
 
@@ -119,8 +175,9 @@ void planInstance(const cxg_problem& pr, const cxg_settings& st, Pools& pools) {
   InstanceDesc D{};
   const int n = pr.n, m = pr.m, p = pr.zero_dim, l = pr.nonneg_dim, nsoc = pr.n_soc;
   const int nr = n + p;
-  // the root scatter maps below hold element offsets of the root in 32-bit ints
-  if (rootSize(nr) > (int64_t)INT32_MAX) throw std::runtime_error("root too large for 32-bit root index maps");
+  // every count the device indexes with a 32-bit int (validateProblem refuses the rest first)
+  const std::string lim = checkPlanCounts(pr);
+  if (!lim.empty()) throw LimitError(lim);
   D.n = n; D.m = m; D.p = p; D.l = l; D.nsoc = nsoc; D.nr = nr;
   D.nnzPu = pr.Pp[n];
   D.nnzA = pr.Ap[n];
@@ -129,7 +186,8 @@ void planInstance(const cxg_problem& pr, const cxg_settings& st, Pools& pools) {
 
   // ---- P: full symmetric CSR over the upper entries, diagonal sources, lower root scatter ----
   std::vector<std::vector<std::pair<int, int>>> rows((size_t)n);
-  std::vector<int> pdiag((size_t)n, -1), plowIdx, plowSrc;
+  std::vector<int> pdiag((size_t)n, -1), plowSrc;
+  std::vector<int64_t> plowIdx;
   for (int c = 0; c < n; ++c)
     for (int k = pr.Pp[c]; k < pr.Pp[c + 1]; ++k) {
       const int r = pr.Pi[k];
@@ -137,7 +195,7 @@ void planInstance(const cxg_problem& pr, const cxg_settings& st, Pools& pools) {
       rows[(size_t)r].push_back({c, k});
       if (r != c) {
         rows[(size_t)c].push_back({r, k});
-        plowIdx.push_back((int)rootIdx(nr, c, r));
+        plowIdx.push_back(rootIdx(nr, c, r));
         plowSrc.push_back(k);
       } else if (pdiag[(size_t)c] < 0) {
         pdiag[(size_t)c] = k;
@@ -157,7 +215,7 @@ void planInstance(const cxg_problem& pr, const cxg_settings& st, Pools& pools) {
   D.iPsCol = pushInts(I, psCol);
   D.iPsSrc = pushInts(I, psSrc);
   D.iPdiag = pushInts(I, pdiag);
-  D.iPlowIdx = pushInts(I, plowIdx);
+  D.iPlowIdx = pushOffsets(I, plowIdx);
   D.iPlowSrc = pushInts(I, plowSrc);
 
   // ---- A: CSC (as given), CSR view, Zero-row root scatter ----
@@ -174,11 +232,12 @@ void planInstance(const cxg_problem& pr, const cxg_settings& st, Pools& pools) {
         arSrc[(size_t)pos] = k;
       }
   }
-  std::vector<int> azIdx, azSrc;
+  std::vector<int64_t> azIdx;
+  std::vector<int> azSrc;
   for (int c = 0; c < n; ++c)
     for (int k = ap[(size_t)c]; k < ap[(size_t)c + 1]; ++k)
       if (ai[(size_t)k] < p) {
-        azIdx.push_back((int)rootIdx(nr, n + ai[(size_t)k], c));
+        azIdx.push_back(rootIdx(nr, n + ai[(size_t)k], c));
         azSrc.push_back(k);
       }
   D.nAZ = (int)azIdx.size();
@@ -187,7 +246,7 @@ void planInstance(const cxg_problem& pr, const cxg_settings& st, Pools& pools) {
   D.iArRow = pushInts(I, arRow);
   D.iArCol = pushInts(I, arCol);
   D.iArSrc = pushInts(I, arSrc);
-  D.iAZIdx = pushInts(I, azIdx);
+  D.iAZIdx = pushOffsets(I, azIdx);
   D.iAZSrc = pushInts(I, azSrc);
 
   // ---- cone units: NN rows then SOC blocks ----
@@ -201,7 +260,7 @@ void planInstance(const cxg_problem& pr, const cxg_settings& st, Pools& pools) {
   const int nUnits = l + nsoc;
   D.nUnits = nUnits;
   std::vector<int> unitAd((size_t)nUnits + 1, 0), unitSup((size_t)nUnits + 1, 0), sup, adSrc;
-  std::vector<std::pair<int, int>> tgtContrib;  // (root index, contribution id)
+  std::vector<std::pair<int64_t, int>> tgtContrib;  // (root element offset, contribution id)
   std::vector<int> contrib;                     // 3 per contribution
   for (int u = 0; u < nUnits; ++u) {
     const int r0 = (u < l) ? p + u : socOff[(size_t)(u - l)];
@@ -227,15 +286,16 @@ void planInstance(const cxg_problem& pr, const cxg_settings& st, Pools& pools) {
         contrib.push_back(adBase + pi * d);
         contrib.push_back(adBase + pj * d);
         contrib.push_back(d);
-        tgtContrib.push_back({(int)rootIdx(nr, S[(size_t)pi], S[(size_t)pj]), cid});
+        tgtContrib.push_back({rootIdx(nr, S[(size_t)pi], S[(size_t)pj]), cid});
       }
     sup.insert(sup.end(), S.begin(), S.end());
     unitAd[(size_t)u + 1] = (int)adSrc.size();
     unitSup[(size_t)u + 1] = (int)sup.size();
   }
   std::stable_sort(tgtContrib.begin(), tgtContrib.end(),
-                   [](const std::pair<int, int>& a, const std::pair<int, int>& b) { return a.first < b.first; });
-  std::vector<int> tgtIdx, tgtBeg, contribSorted;
+                   [](const std::pair<int64_t, int>& a, const std::pair<int64_t, int>& b) { return a.first < b.first; });
+  std::vector<int64_t> tgtIdx;
+  std::vector<int> tgtBeg, contribSorted;
   for (size_t t = 0; t < tgtContrib.size(); ++t) {
     if (t == 0 || tgtContrib[t].first != tgtContrib[t - 1].first) {
       tgtIdx.push_back(tgtContrib[t].first);
@@ -254,7 +314,7 @@ void planInstance(const cxg_problem& pr, const cxg_settings& st, Pools& pools) {
   D.iUnitSup = pushInts(I, unitSup);
   D.iSup = pushInts(I, sup);
   D.iAdSrc = pushInts(I, adSrc);
-  D.iTgtIdx = pushInts(I, tgtIdx);
+  D.iTgtIdx = pushOffsets(I, tgtIdx);
   D.iTgtBeg = pushInts(I, tgtBeg);
   D.iContrib = pushInts(I, contribSorted);
 
@@ -281,6 +341,7 @@ void planInstance(const cxg_problem& pr, const cxg_settings& st, Pools& pools) {
 }
 
 void appendPools(Pools& dst, const Pools& src) {
+  if (dst.ipool.size() & 1) dst.ipool.push_back(0);  // keeps src's 64-bit maps 8-byte aligned
   const int64_t ib = (int64_t)dst.ipool.size(), db = (int64_t)dst.dpool.size();
   dst.ipool.insert(dst.ipool.end(), src.ipool.begin(), src.ipool.end());
   dst.dpool.insert(dst.dpool.end(), src.dpool.begin(), src.dpool.end());

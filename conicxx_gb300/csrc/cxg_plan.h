@@ -3,6 +3,7 @@
 // play in the reference: src/conicxx/kkt/sparsity_map.cpp:8-56, kkt_system.cpp:22-117).
 #pragma once
 
+#include <stdexcept>
 #include <string>
 #include <vector>
 
@@ -22,6 +23,18 @@ struct Pools {
 // dimensions as SolverImpl::setup, solver_impl.cpp:11-16, plus CSC well-formedness, which the
 // device path needs to index safely). Returns an empty string when valid.
 std::string validateProblem(const cxg_problem& pr);
+
+// A size the device plan cannot index (reported as CXG_E_UNSUPPORTED, not as an allocation failure).
+struct LimitError : std::runtime_error {
+  using std::runtime_error::runtime_error;
+};
+
+// The plan's per-instance counts that the device indexes with 32-bit ints, computed exactly from
+// the input pattern before any plan array is built: entries of the full symmetric P (both
+// triangles of the stored upper part), of the densified per-unit A blocks (sum of d_u * s_u over
+// cone units, s_u the number of distinct columns in the unit's rows), and three ints per cone-unit
+// contribution (sum of s_u (s_u + 1) / 2). Returns an empty string when all fit in INT32_MAX.
+std::string checkPlanCounts(const cxg_problem& pr);
 
 // Ruiz equilibration (src/conicxx/kkt/equilibration.cpp:8-100) of the RAW data.
 void computeEquilibration(const cxg_problem& pr, const cxg_settings& st, std::vector<double>& d,

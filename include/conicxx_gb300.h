@@ -290,6 +290,15 @@ int cxg_grid_barrier_selftest(int skip_cta, int rounds, double timeout_s, int* e
 /* Host equilibration of the set-up path (Equilibration::compute, src/conicxx/kkt/equilibration.cpp:8-100):
  * d (n), e (m), c. No GPU needed. */
 int cxg_equilibration(const cxg_problem* problem, const cxg_settings* settings, double* d, double* e, double* c);
+/* Host planning of one instance (the symbolic set-up of KktSystem::setup and SparsityMap,
+ * src/conicxx/kkt/kkt_system.cpp:22-117, sparsity_map.cpp:8-56) without any device work, for
+ * tests of the plan: counts[0..8] = nr, root entries, strictly-upper P scatter entries, Zero-row A
+ * scatter entries, cone-unit target entries, full symmetric P entries, densified A-block entries,
+ * contributions, and 1 when every 64-bit root offset map sits 8-byte aligned in the int pool.
+ * The first `cap` root element offsets of each scatter map go to plow / az / tgt (each nullable).
+ * CXG_E_UNSUPPORTED when a 32-bit plan count would overflow. No GPU needed. */
+int cxg_plan_inspect(const cxg_problem* problem, const cxg_settings* settings, long long* counts, long long* plow,
+                     long long* az, long long* tgt, int cap);
 
 #ifdef __cplusplus
 }

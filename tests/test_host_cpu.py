@@ -170,16 +170,70 @@ def test_whole_gpu_setting_rejections():
     arr = (_abi.Problem * 2)(prob, prob)
     st = _abi.default_settings()
     assert _lib.lib().cxg_batch_create(C.byref(h), 2, arr, C.byref(st)) == _abi.E_UNSUPPORTED
-    # the whole-GPU root's limit: element offsets of the root must fit the 32-bit scatter maps
-    # (64512 rows: 2.147e9 elements; 64513 rows needs a 2017th tile column, 2.149e9 > 2^31 - 1)
-    n = 64513
+    # the whole-GPU root's limit (131072 rows; the scatter maps hold 64-bit root element offsets)
+    n = 131073
     P = Csc.from_coo(n, n, np.arange(n), np.arange(n), np.ones(n))
     A = Csc.from_coo(1, n, [0], [0], [-1.0])
     big = QP(P, np.zeros(n), A, np.ones(1), 0, 1, [])
     prob, keep = make_problem_struct(big)
     st = _abi.default_settings(whole_gpu_root=1)
     assert _lib.lib().cxg_batch_create(C.byref(h), 1, C.byref(prob), C.byref(st)) == _abi.E_UNSUPPORTED
-    assert b"64512" in _lib.lib().cxg_last_error()
+    assert b"131072" in _lib.lib().cxg_last_error()
+
+
+def _root_idx(nr, i, j):
+    """Element offset of root entry (i, j), i >= j: lower triangle of 32x32 tiles in column-major
+    tile order, each tile column-major with leading dimension 33 (the device layout)."""
+    T = -(-nr // 32)
+    I, J = i // 32, j // 32
+    return (J * T - J * (J - 1) // 2 + (I - J)) * 32 * 33 + (j % 32) * 33 + (i % 32)
+
+
+def test_plan_root_offsets_above_2_31():
+    """The plan of a 68000-row root (the full-size group-lasso root, 2.39e9 entries): scatter
+    offsets above 2^31 come out exact and 8-byte aligned in the int pool (host planning only)."""
+    n = 68000
+    rows = list(range(n)) + [n - 2, 100]
+    cols = list(range(n)) + [n - 1, n - 3]
+    P = Csc.from_coo(n, n, rows, cols, np.ones(len(rows)))
+    # Zero row 0 on column n - 10; NN row 1 on columns n - 5, n - 4; SOC (dim 2) rows 2, 3 on n - 7, n - 6
+    A = Csc.from_coo(4, n, [0, 1, 1, 2, 3], [n - 10, n - 5, n - 4, n - 7, n - 6], [1.0, -1.0, -1.0, -1.0, -1.0])
+    qp = QP(P, np.zeros(n), A, np.ones(4), 1, 1, [2])
+    prob, keep = make_problem_struct(qp)
+    st = _abi.default_settings()
+    counts = np.zeros(9, np.int64)
+    cap = 16
+    plow, az, tgt = (np.zeros(cap, np.int64) for _ in range(3))
+    ptr = lambda a: a.ctypes.data_as(_lib.i64p)  # noqa: E731
+    assert _lib.lib().cxg_plan_inspect(C.byref(prob), C.byref(st), ptr(counts), ptr(plow), ptr(az), ptr(tgt), cap) == 0
+    nr = n + 1
+    T = -(-nr // 32)
+    assert counts[0] == nr and counts[1] == T * (T + 1) // 2 * 32 * 33 > 2**31
+    assert counts[8] == 1
+    assert counts[2] == 2 and sorted(plow[:2].tolist()) == sorted([_root_idx(nr, n - 3, 100), _root_idx(nr, n - 1, n - 2)])
+    assert max(plow[:2]) > 2**31
+    assert counts[3] == 1 and az[0] == _root_idx(nr, n, n - 10) and az[0] > 2**31
+    want = sorted({_root_idx(nr, i, j) for (i, j) in [(n - 5, n - 5), (n - 4, n - 5), (n - 4, n - 4),
+                                                         (n - 7, n - 7), (n - 6, n - 7), (n - 6, n - 6)]})
+    assert counts[4] == len(want) and tgt[:len(want)].tolist() == want and min(want) > 2**31
+
+
+def test_plan_counts_beyond_32_bits_refused():
+    """A plan count the device indexes with 32-bit ints is computed from the pattern and refused
+    (CXG_E_UNSUPPORTED) before any plan array or device work: one SOC block of dimension 50000
+    whose rows touch 50000 distinct columns densifies to 2.5e9 A-block entries."""
+    n = 50000
+    P = Csc.from_coo(n, n, np.arange(n), np.arange(n), np.ones(n))
+    A = Csc.from_coo(n, n, np.arange(n), np.arange(n), -np.ones(n))
+    qp = QP(P, np.zeros(n), A, np.concatenate([[1.0], np.zeros(n - 1)]), 0, 0, [n])
+    prob, keep = make_problem_struct(qp)
+    st = _abi.default_settings(whole_gpu_root=1)
+    h = C.c_void_p()
+    assert _lib.lib().cxg_batch_create(C.byref(h), 1, C.byref(prob), C.byref(st)) == _abi.E_UNSUPPORTED
+    assert b"32-bit" in _lib.lib().cxg_last_error()
+    counts = np.zeros(9, np.int64)
+    assert _lib.lib().cxg_plan_inspect(C.byref(prob), C.byref(st), counts.ctypes.data_as(_lib.i64p), None, None, None,
+                                       0) == _abi.E_UNSUPPORTED
 
 
 def test_dense_inputs_convert_like_the_reference():
