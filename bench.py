@@ -318,15 +318,57 @@ def run_gb300(args, rank, world, local_rank):
                   "iterations_gpu": int(sol0.info["iterations"]), "iterations_cpu": int(oi0["iterations"]),
                   "status_gpu": int(sol0.status), "status_cpu": int(oi0["status"])}
         large = large_instance_leg(orc)
+        # ---- the same batch with the FP64 factor (configuration 1 names FP64 and mixed) ----
+        B64 = BatchSolver(qps, settings=default_settings(precision=0, warm_start=0))
+        dx64 = torch.empty_like(dx)
+        ds64 = torch.empty_like(ds)
+        dz64 = torch.empty_like(dz)
+
+        def step64():
+            B64.update_values_device(*(int(t.data_ptr()) for t in dvals), sp)
+            B64.solve_device(int(dx64.data_ptr()), int(ds64.data_ptr()), int(dz64.data_ptr()), sp)
+
+        with torch.cuda.stream(stream):
+            step64()
+            torch.cuda.synchronize()
+            e64 = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+            t64 = []
+            for i in range(2):
+                flush.fill_(i & 0xFF)
+                e64[0].record(stream)
+                step64()
+                e64[1].record(stream)
+                torch.cuda.synchronize()
+                t64.append(e64[0].elapsed_time(e64[1]))
+        infos64 = np.zeros(count, dtype=INFO_DTYPE)
+        B64.solve_device(int(dx64.data_ptr()), int(ds64.data_ptr()), int(dz64.data_ptr()), sp, infos64)
+        torch.cuda.synchronize()
+        fp64_batch = {"value": count / (1e-3 * float(np.median(t64))), "unit": "solves/s",
+                      "ms_per_step": float(np.median(t64)),
+                      "statuses": {int(k): int(v) for k, v in zip(*np.unique(infos64["status"], return_counts=True))}}
         ncpu = os.cpu_count() or 1
         sample = qps[:args.cpu_sample]
-        cpu_wall, cpu_st, _ = orc.batch_solve(sample, ncpu, warm_start=0)
+        cpu_wall, cpu_st, cpu_it, ox, os_, oz = orc.batch_solve_x(sample, ncpu, warm_start=0)
         cpu_rate = len(sample) / cpu_wall
+        # ---- per-instance error against the FP64 oracle on that sample, both precisions ----
+        errors = {"sample": f"first {len(sample)} instances",
+                  "metric": "max |v_gpu - v_oracle| / max(1, max |v_oracle|) per instance, v = x, s, z"}
+        for name, inf_, tx, ts, tz in (("mixed", infos, dx, ds, dz), ("fp64", infos64, dx64, ds64, dz64)):
+            gx, gs, gz = (t.cpu().numpy() for t in (tx, ts, tz))
+            errors[name] = parity_summary(sample, B, inf_[:len(sample)], cpu_st, cpu_it, (gx, gs, gz), (ox, os_, oz))
         # ---- roofline of the IPM launch set (one persistent launch per size bucket, run
         # concurrently; timed by CUDA events around the solve on the launching stream) ----
         hbm_peak, peak_kind = peaks()
         algo_bytes = B.algorithmic_bytes()
         achieved = algo_bytes / (ipm_ms * 1e-3) / 1e9
+        # compute bound: the root LDL' (nr^3/6 multiply-adds per factorisation) and its triangular
+        # solves (nr^2 per solve pair; 3 solves per iteration plus the refinement steps) on the
+        # FP32 CUDA cores, per instance from its iterations and refinement counts
+        nr = np.array([qp_.n + qp_.zero for qp_ in qps], dtype=np.float64)
+        it = infos["iterations"].astype(np.float64)
+        fma = float(np.sum(it * nr ** 3 / 6.0 + (3.0 * it + infos["refine_steps"]) * nr ** 2))
+        tflops = 2.0 * fma / (ipm_ms * 1e-3) / 1e12
+        fp32_peak = 2.0 * 152 * 128 * 2.07e9 / 1e12
         traffic, fp64_pipe = None, None
         tp = os.path.join(ROOT, "profiles", "ipm_kernel_traffic.json")
         if os.path.exists(tp):
@@ -343,12 +385,23 @@ def run_gb300(args, rank, world, local_rank):
                           "sample": f"first {len(sample)} of the {count} instances, one instance per thread, "
                                     f"cold start, FP64 oracle restatement of the reference",
                           "solved_fraction": float(np.mean(cpu_st == 1))},
-            roofline={"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                      "frac": achieved / hbm_peak, "traffic": traffic, "peak_kind": peak_kind,
-                      "ipm_ms": ipm_ms, "algorithmic_bytes": algo_bytes, "fp64_pipe_active_frac": fp64_pipe,
-                      "note": "IPM launch set (one persistent launch per size bucket); algorithmic bytes = "
-                              "plans + problem values + solutions + results read/written once; the kernel is "
-                              "bound by FP64 pipe and barrier latency of the slowest instances, not by HBM"},
+            roofline={"bound": "fp32", "achieved": tflops, "peak": fp32_peak, "unit": "TFLOP/s",
+                      "frac": tflops / fp32_peak, "traffic": traffic,
+                      "peak_kind": "nominal FP32 CUDA-core rate: 152 SMs x 128 FMA/clock x 2.07 GHz (no measured "
+                                   "FP32 figure exists for this pool)",
+                      "ipm_ms": ipm_ms, "multiply_adds": fma, "fp64_pipe_active_frac": fp64_pipe,
+                      "hbm": {"achieved": achieved, "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
+                              "peak_kind": peak_kind, "algorithmic_bytes": algo_bytes},
+                      "note": "IPM launch set (one persistent launch per size bucket). Compute: sum over "
+                              "instances of iterations x nr^3/6 (root LDL') + (3 x iterations + refinement "
+                              "steps) x nr^2 (triangular solves) multiply-adds, 2 flops each; instances that "
+                              "hold the double-float factor spend about 12 FP32 operations per such "
+                              "multiply-add. HBM: plans + values + solutions + results once; the whole "
+                              "problem lives in shared memory and L2 for every iteration, so HBM is not the "
+                              "bound. The makespan is set by the slowest instances' serial FP64/double-float "
+                              "chains"},
+            fp64_batch=fp64_batch,
+            parity_vs_oracle=errors,
             fwd_bwd=fwd_bwd,
             single_instance=single,
             large_instance=large,
@@ -357,6 +410,37 @@ def run_gb300(args, rank, world, local_rank):
     if tune_report is not None:
         result["autotune"] = tune_report.strip().splitlines()
     return ms, wall, clocks, launches_per_step, solved_frac, statuses, result
+
+
+def parity_summary(sample, B, infos, cpu_st, cpu_it, gpu, orc_):
+    """Status agreement, iteration differences and per-instance x/s/z errors of the device batch
+    against the FP64 oracle on the instances of `sample` (the first len(sample) of batch B)."""
+    gx, gs, gz = gpu
+    ox, os_, oz = orc_
+    st_g = infos["status"].astype(int)
+    st_o = np.asarray(cpu_st, int)
+    both = (st_g == 1) & (st_o == 1)
+    errs = {"x": [], "s": [], "z": []}
+    for i, qp in enumerate(sample):
+        if not both[i]:
+            continue
+        # the sample is the batch's first instances, so both concatenations share the offsets
+        for key, g, o, off, ln in (("x", gx, ox, B.n_off[i], qp.n), ("s", gs, os_, B.m_off[i], qp.m),
+                                   ("z", gz, oz, B.m_off[i], qp.m)):
+            ov, gv = o[off:off + ln], g[off:off + ln]
+            errs[key].append(float(np.max(np.abs(gv - ov)) / max(1.0, float(np.max(np.abs(ov))))))
+    dit = (infos["iterations"].astype(int) - np.asarray(cpu_it, int))[both]
+    out = {"status_agree": int(np.sum(st_g == st_o)), "instances": len(sample),
+           "status_mismatches": [[i, int(st_g[i]), int(st_o[i])] for i in np.nonzero(st_g != st_o)[0].tolist()],
+           "both_solved": int(both.sum()),
+           "iterations_equal_frac": float(np.mean(dit == 0)) if dit.size else None,
+           "iterations_within_1_frac": float(np.mean(np.abs(dit) <= 1)) if dit.size else None}
+    for key, v in errs.items():
+        v = np.array(v)
+        if v.size:
+            out[key] = {"median": float(np.median(v)), "p99": float(np.quantile(v, 0.99)), "max": float(v.max()),
+                        "frac_le_1e-6": float(np.mean(v <= 1e-6))}
+    return out
 
 
 def large_instance_leg(orc):
@@ -424,6 +508,44 @@ def large_instance_leg(orc):
     return out
 
 
+def ldlt_probe(nr, nx, arith, threads, seed=1, check=False):
+    """The dense root LDL' and triangular solve alone (cxg_dense_ldlt) on a seeded quasi-definite
+    matrix of the reduced-KKT shape [P, A_Z'; A_Z, -0.5 I]: P = B B'/nx + I (nx x nx), A_Z ~ 0.5
+    N(0,1). threads -1 runs the whole-GPU root (every SM); 32..256 the one-CTA root. Returns factor
+    and solve time (ns from the device timer, or SM cycles for one CTA), multiply-adds per second,
+    the pivot flags and, with check, the relative error against a float64 solve."""
+    from conicxx_gb300 import _abi, _lib
+
+    rng = np.random.default_rng(seed)
+    B = rng.standard_normal((nx, nx))
+    K = np.zeros((nr, nr), order="F")
+    K[:nx, :nx] = B @ B.T / nx + np.eye(nx)
+    AZ = rng.standard_normal((nr - nx, nx)) * 0.5
+    K[nx:, :nx] = AZ
+    K[:nx, nx:] = AZ.T
+    K[nx:, nx:] = -0.5 * np.eye(nr - nx)
+    b = np.random.default_rng(seed + 1).standard_normal(nr)
+    D, x = np.zeros(nr), np.zeros(nr)
+    cyc = np.zeros(2, np.int64)
+    flags = np.zeros(3, np.int32)
+    code = {"fp64": 0, "fp32": 1, "df64": 2}[arith]
+    rc = _lib.lib().cxg_dense_ldlt(nr, nx, K.ctypes.data, b.ctypes.data, code, threads, _abi.LINSOLVER_QDLDL,
+                                   None, D.ctypes.data, x.ctypes.data, cyc.ctypes.data, flags.ctypes.data)
+    if rc != _abi.OK:
+        raise RuntimeError(_lib.lib().cxg_last_error().decode())
+    out = {"probe": "dense root LDL'", "nr": nr, "nx": nx, "arith": arith, "threads": threads,
+           "flags": flags.tolist()}
+    fma = nr ** 3 / 6.0
+    if threads < 0:
+        out.update(ldlt_ms=cyc[0] / 1e6, solve_ms=cyc[1] / 1e6, ldlt_fma_per_s=fma / (cyc[0] * 1e-9))
+    else:
+        out.update(ldlt_cycles=int(cyc[0]), solve_cycles=int(cyc[1]))
+    if check:
+        xs = np.linalg.solve(K, b)
+        out["x_rel_err"] = float(np.linalg.norm(x - xs) / np.linalg.norm(xs))
+    return out
+
+
 def run_reference(args, rank, world):
     """The reference's CPU path: the FP64 oracle restatement (the reference itself cannot be
     built in this environment), all host threads, one instance per thread."""
@@ -475,8 +597,24 @@ def main():
                          "entry point (direct launches, buckets in sequence)")
     ap.add_argument("--legs", default="all", choices=["all", "main"],
                     help="main: only the device-resident batched timing (profiling runs)")
+    ap.add_argument("--probe-ldlt", type=int, default=0, metavar="NR",
+                    help="instead of the benchmark: time the dense root LDL' alone on an NR-row matrix")
+    ap.add_argument("--probe-arith", default="fp32", choices=["fp64", "fp32", "df64"])
+    ap.add_argument("--probe-threads", type=int, default=-1, help="-1: whole-GPU root; 32..256: one CTA")
+    ap.add_argument("--probe-repeat", type=int, default=1)
+    ap.add_argument("--probe-check", action="store_true")
     args = ap.parse_args()
     rank, world, local_rank = dist_env()
+    if args.probe_ldlt:
+        if not os.path.exists(os.path.join(ROOT, "conicxx_gb300", "_build", "libconicxx_gb300.so")):
+            import __graft_entry__
+
+            __graft_entry__.build()
+        nr = args.probe_ldlt
+        for _ in range(args.probe_repeat):
+            print(json.dumps(ldlt_probe(nr, max(1, nr - 256), args.probe_arith, args.probe_threads,
+                                        check=args.probe_check)), flush=True)
+        return
     if args.impl == "reference":
         out = run_reference(args, rank, world)
         if out is not None:

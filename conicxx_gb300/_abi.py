@@ -56,6 +56,8 @@ class Settings(C.Structure):
         ("threads_per_instance", C.c_int),
         ("differentiable", C.c_int),
         ("whole_gpu_root", C.c_int),
+        ("fault_factor_failures", C.c_int),
+        ("fault_nonfinite_solves", C.c_int),
     ]
 
 
@@ -69,7 +71,7 @@ def default_settings(**overrides):
         warm_start=1, verbose=0, record_timings=0, validate_inputs=1,
         linear_solver=LINSOLVER_QDLDL, precision=PRECISION_FP64, mixed_refine_max_iter=4,
         mixed_fallback_tol=1e-10, threads_per_instance=0, differentiable=0,
-        whole_gpu_root=0,
+        whole_gpu_root=0, fault_factor_failures=0, fault_nonfinite_solves=0,
     )
     for k, v in overrides.items():
         if not hasattr(s, k):
@@ -104,6 +106,7 @@ class Info(C.Structure):
         ("factor_attempts", C.c_int),
         ("time_start_s", C.c_double),
         ("time_end_s", C.c_double),
+        ("escalations", C.c_int),
     ]
 
     def as_dict(self):

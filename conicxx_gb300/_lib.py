@@ -51,6 +51,8 @@ SIGNATURES = {
     "cxg_batch_backward": (C.c_int, [vp, dp, dp, dp, dp, dp]),
     "cxg_batch_backward_device": (C.c_int, [vp, vp, vp, vp, vp, vp, vp]),
     "cxg_batch_last_launches": (C.c_int, [vp]),
+    "cxg_batch_trace": (C.c_int, [vp, C.c_int, dp, C.c_int]),
+    "cxg_solver_trace": (C.c_int, [vp, dp, C.c_int]),
     "cxg_batch_describe": (C.c_int, [vp, C.c_char_p, C.c_int]),
     "cxg_batch_footprint": (C.c_int, [vp, i64p, i64p, i64p]),
     "cxg_cones_eval": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, ip, dp, dp, dp, dp, C.c_double, dp, dp, dp]),

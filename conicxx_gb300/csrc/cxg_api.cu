@@ -98,6 +98,8 @@ extern "C" void cxg_default_settings(cxg_settings* s) {
   s->threads_per_instance = 0;
   s->differentiable = 0;
   s->whole_gpu_root = 0;
+  s->fault_factor_failures = 0;
+  s->fault_nonfinite_solves = 0;
 }
 
 // ------------------------------------------------------------------------------------------
@@ -153,12 +155,14 @@ struct cxg_batch {
   bool gridMode = false;                    // one instance, root spread over every SM (launchIpmGrid)
   bool bwdDropped = false;                  // differentiable asked for, not kept (whole-GPU root > 8192 rows)
   void* dGridCtl = nullptr;                 // its control block
+  double* dTrace = nullptr;                 // record_timings: iteration traces (count x traceRows rows)
+  int traceRows = 0;
 
   ~cxg_batch() {
     if (graphExec) cudaGraphExecDestroy(graphExec);
     if (graph) cudaGraphDestroy(graph);
     void* ptrs[] = {dDesc, dIpool, dDpool, dPx, dq, dAx, db, dx, ds, dz, dRes, dWx, dWs, dWz, dHaveWarm, dScratch,
-                    dCounters, dOrder, dBwd, dGx, dGq, dGb, dGP, dGA, dGridCtl};
+                    dCounters, dOrder, dBwd, dGx, dGq, dGb, dGP, dGA, dGridCtl, dTrace};
     for (void* p : ptrs)
       if (p) cudaFree(p);
     for (cudaEvent_t e : forkJoin) cudaEventDestroy(e);
@@ -188,6 +192,8 @@ static DevSettings makeDevSettings(const cxg_settings& st, const cxg_settings& k
   d.warm_start = st.warm_start;
   d.precision = st.precision;
   d.record_timings = st.record_timings ? 1 : 0;
+  d.fault_factor_failures = std::max(st.fault_factor_failures, 0);
+  d.fault_nonfinite_solves = std::max(st.fault_nonfinite_solves, 0);
   return d;
 }
 
@@ -320,6 +326,7 @@ static int buildGroups(cxg_batch* B) {
       D.sRoot64 = o; o += needRoot64 ? r2(rootSize(D.nr)) : 0;
       D.sVec = o; o += L.vecInSmem ? 0 : vecDoubles(L.nMax, L.mMax, L.nrMax, L.nsocMax);
       D.sVecG = o; o += vecGlobalDoubles(L.mMax);
+      D.sKry = o; o += gridMode ? krylovDoubles(L.nMax, L.mMax) : 0;
       D.scratchDoubles = o;
       stride = std::max(stride, o);
     }
@@ -617,11 +624,30 @@ static LaunchArgs solveArgs(const cxg_batch* B, const Group& g, const DevSetting
   a.warmZ = B->dWz;
   a.haveWarm = B->dHaveWarm;
   a.bwd = B->dBwd;
+  a.trace = ds.record_timings ? B->dTrace : nullptr;
+  a.traceRows = B->traceRows;
   a.scratch = scratch;
   a.scratchStride = g.stride;
   a.st = ds;
   a.lay = g.lay;
   return a;
+}
+
+// record_timings: the iteration-trace buffer, sized for max_iter rows per instance (allocated
+// before any graph capture; a larger max_iter re-allocates it and invalidates the graph).
+static int ensureTrace(cxg_batch* B) {
+  if (!B->st.record_timings) return CXG_OK;
+  const int rows = std::max(1, B->st.max_iter);
+  if (B->dTrace && B->traceRows >= rows) return CXG_OK;
+  if (B->dTrace) cudaFree(B->dTrace);
+  B->dTrace = nullptr;
+  B->traceRows = 0;
+  B->graphValid = false;
+  int rc = devAlloc(&B->dTrace, (size_t)B->count * (size_t)rows * kTraceCols);
+  if (rc) return rc;
+  CX_CUDA(cudaMemset(B->dTrace, 0, sizeof(double) * (size_t)B->count * (size_t)rows * kTraceCols));
+  B->traceRows = rows;
+  return CXG_OK;
 }
 
 // ------------------------------------------------------------------------------------------
@@ -753,6 +779,7 @@ static int enqueueSolve(cxg_batch* B, cudaStream_t s) {
 
 // Device-side solve through the captured graph (re-captured when the settings change).
 static int runSolve(cxg_batch* B, cudaStream_t s) {
+  if (int rc = ensureTrace(B)) return rc;
   // the whole-GPU form is one cooperative launch: enqueued directly, not through a graph
   if (B->gridMode) return enqueueSolve(B, s);
   const DevSettings ds = makeDevSettings(B->st, B->kktSt);
@@ -794,6 +821,7 @@ static void resultToInfo(const DevResult& R, cxg_info& I, double setupTime, doub
   I.refine_steps = R.refine_steps;
   I.max_relres = R.max_relres;
   I.factor_attempts = R.factor_attempts;
+  I.escalations = R.escalations;
   if (g_clockHz > 0.0) {
     I.time_factor_s = (double)R.cycles[1] / g_clockHz;
     I.time_kkt_solve_s = (double)R.cycles[2] / g_clockHz;
@@ -1292,7 +1320,11 @@ extern "C" int cxg_batch_solve_device_noalloc(cxg_batch* B, double* x, double* s
     const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(g.grid, capDoubles / g.stride));
     CX_CUDA(launchIpm(a, grid, g.block, g.smem, g.fp32, st));
   }
-  B->lastLaunches = (int)G;
+  // history-ordered queues for the next solve, as the other solve entry points keep them (the
+  // re-ordering kernel uses static shared memory and the batch's own queue array only)
+  rc = enqueueReorder(B, st);
+  if (rc) return rc;
+  B->lastLaunches = (int)G + ((G >= 1 && G <= (size_t)kMaxGroups) ? 1 : 0);
   if (x && B->pools.totQ) CX_CUDA(cudaMemcpyAsync(x, B->dx, (size_t)B->pools.totQ * 8, cudaMemcpyDeviceToDevice, st));
   if (s && B->pools.totB) CX_CUDA(cudaMemcpyAsync(s, B->ds, (size_t)B->pools.totB * 8, cudaMemcpyDeviceToDevice, st));
   if (z && B->pools.totB) CX_CUDA(cudaMemcpyAsync(z, B->dz, (size_t)B->pools.totB * 8, cudaMemcpyDeviceToDevice, st));
@@ -1301,4 +1333,26 @@ extern "C" int cxg_batch_solve_device_noalloc(cxg_batch* B, double* x, double* s
     return fetchInfo(B, info, 0.0);
   }
   return CXG_OK;
+}
+
+static int traceCopy(cxg_batch* B, int instance, double* out, int capRows) {
+  if (!B || !out || capRows < 0) return setErr(CXG_E_INVALID, "null argument");
+  if (instance < 0 || instance >= B->count) return setErr(CXG_E_INVALID, "instance index out of range");
+  if (!B->dTrace) return setErr(CXG_E_INVALID, "no trace: solve with record_timings set first");
+  DevResult R{};
+  CX_CUDA(cudaMemcpy(&R, B->dRes + instance, sizeof(DevResult), cudaMemcpyDeviceToHost));
+  const int rows = std::min({R.iterations, B->traceRows, capRows});
+  if (rows > 0)
+    CX_CUDA(cudaMemcpy(out, B->dTrace + (size_t)instance * B->traceRows * kTraceCols,
+                       sizeof(double) * (size_t)rows * kTraceCols, cudaMemcpyDeviceToHost));
+  return rows;
+}
+
+extern "C" int cxg_batch_trace(cxg_batch* B, int instance, double* out, int cap_rows) {
+  return traceCopy(B, instance, out, cap_rows);
+}
+
+extern "C" int cxg_solver_trace(cxg_solver* S, double* out, int cap_rows) {
+  if (!S || !S->setupDone || !S->batch) return setErr(CXG_E_INVALID, "solver not set up");
+  return traceCopy(S->batch, 0, out, cap_rows);
 }

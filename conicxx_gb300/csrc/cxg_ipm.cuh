@@ -135,13 +135,14 @@ struct Ctx {
   double* red;
   int* redi;
   double* sc;      // scalar broadcast area
+  double* kry;     // whole-GPU form: GMRES Krylov area (krylovDoubles) in scratch
   GridCtl* grid;   // whole-GPU launch: the root jobs run on every CTA (null: this CTA alone)
 };
 
 // scalar slots in Ctx::sc
 enum {
   SC_TAU = 0, SC_KAPPA, SC_EXTRA_P, SC_EXTRA_A, SC_USE64, SC_NFB, SC_RSTEPS, SC_MAXREL,
-  SC_ATTEMPTS, SC_FACTOK, SC_COUNT
+  SC_ATTEMPTS, SC_FACTOK, SC_GMRES, SC_ITREL, SC_FAULTF, SC_FAULTS, SC_ESC, SC_COUNT
 };
 
 // Phase cycle counters (record_timings), kept by thread 0 in the scalar area after PivotStats.
@@ -352,6 +353,29 @@ static __device__ __noinline__ double kktResidualImpl(Ctx& c, const DevSettings&
   blockSum<2>(acc2, c.red);
   rhsNorm = fmax(sqrt(acc2[1]), 1e-30);
   return sqrt(acc2[0]) / rhsNorm;
+}
+
+// y = K sol for the same statically regularised K (the operator of the GMRES refinement).
+static __device__ __noinline__ void kktApply(Ctx& c, const DevSettings& st, const double* sol, double* y) {
+  const int n = c.n, m = c.m;
+  const double* xs = sol;
+  const double* zs = sol + n;
+  FOR_T(t, n + m) {
+    if (t < n) {
+      double acc = st.static_reg_P * xs[t] + csrDot(c.Pv, c.psCol, c.psRow[t], c.psRow[t + 1], xs);
+      acc += csrDot(c.Av, c.ai, c.ap[t], c.ap[t + 1], zs);
+      y[t] = acc;
+    } else {
+      const int r = t - n;
+      double acc = 0.0;
+      for (int k = c.arRow[r]; k < c.arRow[r + 1]; ++k) acc += c.Av[c.arSrc[k]] * xs[c.arCol[k]];
+      y[t] = acc;
+    }
+  }
+  __syncthreads();
+  coneApply(c, kHsEps, st.static_reg_A, zs, c.tm2);
+  FOR_T(r, m) y[n + r] -= c.tm2[r];
+  __syncthreads();
 }
 
 static __device__ double kktResidual(Ctx& c, const DevSettings& st, const double* rhs, const double* sol, double* res,
@@ -1671,6 +1695,13 @@ __device__ __noinline__ bool factorizeWithRetryImpl(Ctx& c, const DevSettings& s
       assembleFactor<typename HighT<FT>::type, G>(c, st, rootHigh<FT>(c), ep, ea, fail, wrong, mind);
     }
     if (threadIdx.x == 0) c.sc[SC_ATTEMPTS] += 1.0;
+    // fault injection (tests): this attempt reports failure
+    const bool injected = c.sc[SC_FAULTF] < (double)st.fault_factor_failures;
+    __syncthreads();
+    if (injected) {
+      if (threadIdx.x == 0) c.sc[SC_FAULTF] += 1.0;
+      fail = 1;
+    }
     if (!fail && isfinite(mind) && mind > st.dynamic_reg_eps) {
       fs.ep = ep;
       fs.ea = ea;
@@ -1682,18 +1713,135 @@ __device__ __noinline__ bool factorizeWithRetryImpl(Ctx& c, const DevSettings& s
   return false;
 }
 
-template <typename FT, bool G = false>
+template <typename FT, bool G>
 __device__ void solveOnce(Ctx& c, const DevSettings& st, const FactState& fs, const double* rhs, double* sol) {
   if (fs.use64)
     reducedSolve<typename HighT<FT>::type, G>(c, st, rootHigh<FT>(c), fs.ea, rhs, sol);
   else
     reducedSolve<FT, G>(c, st, rootT<FT>(c), fs.ea, rhs, sol);
+  // fault injection (tests): this solve returns a non-finite vector
+  if (st.fault_nonfinite_solves > 0) {
+    const bool injected = c.sc[SC_FAULTS] < (double)st.fault_nonfinite_solves;
+    __syncthreads();
+    if (injected && threadIdx.x == 0) {
+      c.sc[SC_FAULTS] += 1.0;
+      sol[0] = NAN;
+    }
+    __syncthreads();
+  }
 }
 
 static __device__ __noinline__ bool vecFinite(Ctx& c, const double* v, int len) {
   int bad = 0;
   FOR_T(i, len) bad |= !finiteBits(v[i]);
   return blockOrInt(bad, c.redi) == 0;
+}
+
+// Refinement of the whole-GPU form: restarted GMRES in FP64 on the statically regularised K
+// (the matrix the reference refines against, kkt_system.cpp:296-311), right-preconditioned by
+// the held factor (FP32, double-float or FP64 LDL' of the bumped reduced system). Where a
+// large root is ill-conditioned enough that plain refinement x += K^-1 (rhs - K x) with that
+// factor stalls or diverges (the factor's relative error times cond(K) near or above 1), GMRES
+// still converges, in a few iterations per cluster of poorly resolved eigenvalues (the mixed
+// precision GMRES-IR of Carson and Higham, SIAM J. Sci. Comput. 40(2), 2018). Each iteration is one
+// solve with the factor (every SM), one K product and modified Gram-Schmidt (CTA 0). On entry
+// sol is the first solve and c.res = rhs - K sol with relative norm rel; a cycle's correction is
+// kept only if the true residual drops. Returns the final relative residual; counts iterations
+// in SC_RSTEPS.
+template <typename FT, bool G>
+__device__ void solveOnce(Ctx& c, const DevSettings& st, const FactState& fs, const double* rhs, double* sol);
+
+template <typename FT, bool G>
+__device__ __noinline__ double gmresRefine(Ctx& c, const DevSettings& st, const FactState& fs, const double* rhs,
+                                           double* sol, double rel, double rhsNorm) {
+  const int N = c.n + c.m;
+  const int64_t ld = ((int64_t)N + 1) & ~int64_t(1);
+  constexpr int hl = kGmresDim + 1;  // leading dimension of H (column-major)
+  double* V = c.kry;
+  double* Z = V + (int64_t)(kGmresDim + 1) * ld;
+  double* H = Z + (int64_t)kGmresDim * ld;
+  double* cs = H + hl * kGmresDim;
+  double* sn = cs + kGmresDim;
+  double* g = sn + kGmresDim;
+  double* y = g + kGmresDim + 1;
+  int total = 0;
+  for (int cyc = 0; cyc < kGmresCycles && rel > st.refine_tol; ++cyc) {
+    const double beta = rel * rhsNorm;
+    FOR_T(i, N) V[i] = c.res[i] / beta;
+    if (threadIdx.x == 0) g[0] = beta;
+    __syncthreads();
+    int k = 0;
+    for (int j = 0; j < kGmresDim; ++j) {
+      double* vj = V + (int64_t)j * ld;
+      double* zj = Z + (int64_t)j * ld;
+      solveOnce<FT, G>(c, st, fs, vj, zj);
+      double* w = V + (int64_t)(j + 1) * ld;
+      kktApply(c, st, zj, w);
+      for (int i = 0; i <= j; ++i) {
+        const double* vi = V + (int64_t)i * ld;
+        double d[1] = {0.0};
+        FOR_T(t, N) d[0] += w[t] * vi[t];
+        blockSum<1>(d, c.red);
+        FOR_T(t, N) w[t] -= d[0] * vi[t];
+        if (threadIdx.x == 0) H[j * hl + i] = d[0];
+        __syncthreads();
+      }
+      double nn[1] = {0.0};
+      FOR_T(t, N) nn[0] += w[t] * w[t];
+      blockSum<1>(nn, c.red);
+      const double hn = sqrt(nn[0]);
+      if (threadIdx.x == 0) {
+        double* h = H + j * hl;
+        h[j + 1] = hn;
+        for (int i = 0; i < j; ++i) {
+          const double t = cs[i] * h[i] + sn[i] * h[i + 1];
+          h[i + 1] = -sn[i] * h[i] + cs[i] * h[i + 1];
+          h[i] = t;
+        }
+        const double den = hypot(h[j], h[j + 1]);
+        const double cj = den > 0.0 ? h[j] / den : 1.0, sj = den > 0.0 ? h[j + 1] / den : 0.0;
+        cs[j] = cj;
+        sn[j] = sj;
+        h[j] = den;
+        h[j + 1] = 0.0;
+        g[j + 1] = -sj * g[j];
+        g[j] = cj * g[j];
+        c.sc[SC_GMRES] = fabs(g[j + 1]) / rhsNorm;
+      }
+      __syncthreads();
+      k = j + 1;
+      // stop at a residual estimate well below the target (the true residual is checked below),
+      // or at breakdown (the Krylov space holds the solution)
+      if (!(hn > 0.0) || !(c.sc[SC_GMRES] > 0.25 * st.refine_tol)) break;
+      const double inv = 1.0 / hn;
+      FOR_T(t, N) w[t] *= inv;
+      __syncthreads();
+    }
+    total += k;
+    if (threadIdx.x == 0) {
+      for (int i = k - 1; i >= 0; --i) {
+        double acc = g[i];
+        for (int l = i + 1; l < k; ++l) acc -= H[l * hl + i] * y[l];
+        y[i] = acc / H[i * hl + i];
+      }
+    }
+    __syncthreads();
+    FOR_T(t, N) {
+      double acc = sol[t];
+      for (int l = 0; l < k; ++l) acc += y[l] * Z[(int64_t)l * ld + t];
+      c.cor[t] = acc;
+    }
+    __syncthreads();
+    double rn = 1.0;
+    const double relNew = kktResidual(c, st, rhs, c.cor, c.res, rn);
+    if (!(relNew < rel)) break;  // no progress (or a non-finite candidate): keep sol
+    FOR_T(t, N) sol[t] = c.cor[t];
+    __syncthreads();
+    rel = relNew;
+  }
+  if (threadIdx.x == 0) c.sc[SC_RSTEPS] += total;
+  __syncthreads();
+  return rel;
 }
 
 // KktSystem::solve (kkt_system.cpp:296-311) incl. escalateAndResolve (:266-294), plus the
@@ -1715,6 +1863,7 @@ __device__ __noinline__ double kktSolveImpl(Ctx& c, const DevSettings& st, FactS
         ea = fmax(ea * 1000.0, st.dynamic_reg_delta);
         int fail = 0, wrong = 0;
         double mind = 0.0;
+        if (threadIdx.x == 0) c.sc[SC_ESC] += 1.0;
         if (fs.use64)
           assembleFactor<typename HighT<FT>::type, G>(c, st, rootHigh<FT>(c), ep, ea, fail, wrong, mind);
         else
@@ -1729,7 +1878,10 @@ __device__ __noinline__ double kktSolveImpl(Ctx& c, const DevSettings& st, FactS
     double rhsNorm = 1.0;
     double rel = kktResidual(c, st, rhs, sol, c.res, rhsNorm);
     const bool fp32Factor = (sizeof(FT) == 4) && !fs.use64;
-    const int maxRef = fp32Factor ? st.mixed_refine_max_iter : st.refine_max_iter;
+    const int maxRef = G ? 0 : (fp32Factor ? st.mixed_refine_max_iter : st.refine_max_iter);
+    if constexpr (G) {
+      if (rel > st.refine_tol) rel = gmresRefine<FT, G>(c, st, fs, rhs, sol, rel, rhsNorm);
+    }
     int steps = 0;
     for (int it = 0; it < maxRef && rel > st.refine_tol; ++it) {
       solveOnce<FT, G>(c, st, fs, c.res, c.cor);
@@ -1761,6 +1913,7 @@ __device__ __noinline__ double kktSolveImpl(Ctx& c, const DevSettings& st, FactS
     }
     if (threadIdx.x == 0) {
       if (!(rel <= c.sc[SC_MAXREL])) c.sc[SC_MAXREL] = rel;
+      if (!(rel <= c.sc[SC_ITREL])) c.sc[SC_ITREL] = rel;
     }
     __syncthreads();
     return rel;
@@ -1779,9 +1932,11 @@ __device__ bool factorizeWithRetry(Ctx& c, const DevSettings& st, FactState& fs)
 template <typename FT, bool G = false>
 __device__ double kktSolve(Ctx& c, const DevSettings& st, FactState& fs, const double* rhs, double* sol) {
   const long long t0 = st.record_timings ? clock64() : 0;
-  // the fallback path inside refactors; its time is counted as solve time
+  const long long f0 = st.record_timings ? timers(c)[TM_FACTOR] : 0;
+  __syncthreads();
+  // a fallback refactorisation inside counts as factorisation time only
   const double r = kktSolveImpl<FT, G>(c, st, fs, rhs, sol);
-  if (st.record_timings && threadIdx.x == 0) timers(c)[TM_SOLVE] += clock64() - t0;
+  if (st.record_timings && threadIdx.x == 0) timers(c)[TM_SOLVE] += (clock64() - t0) - (timers(c)[TM_FACTOR] - f0);
   return r;
 }
 
@@ -1859,11 +2014,22 @@ __device__ __noinline__ void solveInstance(Ctx& c, const LaunchArgs& a, int inst
   }
   if (!initOk) status = 5;
 
+  // record_timings: one trace row per iteration (columns as kTraceCols), written by thread 0
+  double* trow = nullptr;
   for (int iter = 0; initOk && iter < st.max_iter; ++iter) {
     iterations = iter + 1;
+    trow = (a.trace && iter < a.traceRows) ? a.trace + ((int64_t)inst * a.traceRows + iter) * kTraceCols : nullptr;
+    if (threadIdx.x == 0) {
+      c.sc[SC_ITREL] = 0.0;
+      if (trow)
+        for (int k = 0; k < kTraceCols; ++k) trow[k] = 0.0;
+    }
+    const double att0 = c.sc[SC_ATTEMPTS];
+    __syncthreads();
     // 1. refactorise for the current scaling
     coneUpdateScaling(c, c.s, c.z);
     if (!factorizeWithRetry<FT, G>(c, st, fs)) { status = 5; break; }
+    if (trow && threadIdx.x == 0) trow[11] = c.sc[SC_ATTEMPTS] - att0;
     // 2. constant solve (-q, b) -> x1, z1; Px1
     FOR_T(j, n) c.rhs[j] = -c.qs[j];
     FOR_T(r, m) c.rhs[n + r] = c.bs[r];
@@ -1909,6 +2075,9 @@ __device__ __noinline__ void solveInstance(Ctx& c, const LaunchArgs& a, int inst
       const double pobj = (0.5 * dxPx / tau + dqx) / tau;
       const double dobj = (-0.5 * dxPx / tau - dbz) / tau;
       // 4. convergence / infeasibility (solver_impl.cpp checkConvergence / checkInfeasibility)
+      if (trow && threadIdx.x == 0) {
+        trow[0] = mu; trow[1] = nrx; trow[2] = nrz; trow[3] = pobj; trow[4] = dobj; trow[8] = tau; trow[9] = kappa;
+      }
       const double gapAbs = fabs(pobj - dobj);
       const double gapTol = st.tol_gap_abs + st.tol_gap_rel * fmax(fabs(pobj), fabs(dobj));
       if (nrx < st.tol_feas && nrz < st.tol_feas && gapAbs < gapTol && tau > 1e-6) { status = 1; break; }
@@ -1985,6 +2154,7 @@ __device__ __noinline__ void solveInstance(Ctx& c, const LaunchArgs& a, int inst
       } else {
         sigma = 1.0;
       }
+      if (trow && threadIdx.x == 0) { trow[5] = aaff; trow[6] = sigma; }
       // 7. combined step: lambda = W z; ds_comb = lambda o lambda + (W^-1 ds_aff) o (W dz_aff) - sigma mu e
       coneApply(c, kW, 0.0, c.z, c.lam);
       coneProduct(c, false, c.lam, c.lam, c.tm);           // lambda o lambda
@@ -2033,6 +2203,7 @@ __device__ __noinline__ void solveInstance(Ctx& c, const LaunchArgs& a, int inst
       alpha = coneMaxStep(c, c.z, c.dz, alpha);
       alpha = coneMaxStep(c, c.s, c.ds, alpha);
       alpha *= st.max_step_fraction;
+      if (trow && threadIdx.x == 0) { trow[7] = alpha; trow[10] = c.sc[SC_ITREL]; }
       if (!isfinite(alpha) || alpha <= 0.0) { status = 5; break; }
       // 9. update and rescale
       FOR_T(j, n) c.x[j] += alpha * c.dx[j];
@@ -2057,6 +2228,7 @@ __device__ __noinline__ void solveInstance(Ctx& c, const LaunchArgs& a, int inst
       }
     }
   }
+  if (trow && threadIdx.x == 0) trow[10] = c.sc[SC_ITREL];  // the last row, whichever way it ended
 
   // finalizeSolution (solver_impl.cpp:342-365 of the reference numbering)
   const bool infeas = (status == 2 || status == 3);
@@ -2130,6 +2302,7 @@ __device__ __noinline__ void solveInstance(Ctx& c, const LaunchArgs& a, int inst
     R.fp64_fallbacks = (int)c.sc[SC_NFB];
     R.refine_steps = (int)c.sc[SC_RSTEPS];
     R.factor_attempts = (int)c.sc[SC_ATTEMPTS];
+    R.escalations = (int)c.sc[SC_ESC];
     R.error_code = (G && reinterpret_cast<volatile GridCtl*>(c.grid)->error) ? 1 : 0;
     const long long tot = clock64() - tStart;
     R.cycles[0] = tot;
@@ -2195,6 +2368,7 @@ static __device__ void setupCtx(Ctx& c, const LaunchArgs& a, int inst, unsigned 
   c.root = L.rootInSmem ? reinterpret_cast<void*>(smem + L.rootOff) : reinterpret_cast<void*>(c.root64);
   c.red = reinterpret_cast<double*>(smem + L.redOff);
   c.sc = c.red + 128;
+  c.kry = scratch + D.sKry;
   c.redi = sRedi;
   c.grid = nullptr;
 }

@@ -29,6 +29,21 @@ inline int64_t vecDoubles(int nMax, int mMax, int nrMax, int nsocMax) {
 // in the CTA's scratch so the shared-memory vector area stays small enough for the largest root.
 inline int64_t vecGlobalDoubles(int mMax) { return 2 * ((int64_t)(mMax + 1) & ~int64_t(1)); }
 
+// Columns of one iteration-trace row (the oracle's trace columns): mu, ||rx||/tau, ||rz||/tau,
+// primal and dual objective, affine step, sigma, step, tau, kappa, the iteration's largest relative
+// KKT residual, and the factorisation attempts of the iteration's refactorisation.
+constexpr int kTraceCols = 12;
+
+// Restarted GMRES refinement of the whole-GPU form: basis dimension per cycle and cycles.
+constexpr int kGmresDim = 20;
+constexpr int kGmresCycles = 3;
+// Doubles of its Krylov area (CTA 0's scratch): V (kGmresDim + 1 vectors of n + m), Z (kGmresDim
+// vectors), the Hessenberg matrix, the Givens rotations, the rotated right-hand side, y.
+inline int64_t krylovDoubles(int nMax, int mMax) {
+  const int64_t ld = ((int64_t)nMax + mMax + 1) & ~int64_t(1);
+  return (2 * kGmresDim + 1) * ld + (kGmresDim + 1) * kGmresDim + 4 * kGmresDim + 2;
+}
+
 struct LaunchArgs {
   const InstanceDesc* desc;
   const int* order;       // instances of this launch, heaviest first
@@ -54,6 +69,8 @@ struct LaunchArgs {
   double* gb;
   double* gP;
   double* gA;
+  double* trace;          // record_timings: per-instance iteration trace (traceRows x kTraceCols), or null
+  int traceRows;
   double* scratch;        // gridDim.x * scratchStride doubles
   int64_t scratchStride;
   DevSettings st;

@@ -85,6 +85,7 @@ struct InstanceDesc {
   int64_t sRoot64;                    // FP64 root (fallback / FP64 precision when not in SMEM)
   int64_t sVec;                       // FP64 vectors that do not fit in shared memory
   int64_t sVecG;                      // FP64 vectors always kept in scratch (vecGlobalDoubles)
+  int64_t sKry;                       // whole-GPU form: the GMRES Krylov area (krylovDoubles)
   int64_t scratchDoubles;             // total per-CTA scratch this instance needs
   int64_t bwdOff;                     // offset of this instance's saved final state (differentiable)
   double cost;                        // scheduling weight (~ nr^3)
@@ -117,6 +118,7 @@ struct DevSettings {
   double refine_tol, max_step_fraction, mixed_fallback_tol;
   int max_iter, refine_max_iter, mixed_refine_max_iter, linear_solver;
   int equilibrate, warm_start, precision, record_timings;
+  int fault_factor_failures, fault_nonfinite_solves;  // test-only fault injection (0 = off)
 };
 
 // Per-instance result written by the kernel (mirrors cxg_info plus internal counters).
@@ -124,6 +126,7 @@ struct DevResult {
   int status, iterations, fp64_fallbacks, refine_steps;
   double objective, primal_residual, dual_residual, duality_gap, mu, max_relres;
   int factor_attempts, error_code;  // error_code: 0 ok, else an internal diagnostic (bounds etc.)
+  int escalations, pad1;            // refactorisations of escalateAndResolve (x1000 bumps)
   long long cycles[8];              // record_timings: total, factorisation, KKT solves, residual/cones,
                                     // assembly, dense LDL', dense triangular solves, KKT residuals
   long long wall_ns[2];             // record_timings: device global timer at the instance's start and end

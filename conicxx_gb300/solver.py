@@ -16,6 +16,11 @@ from ._abi import Info, Settings, default_settings, dptr, iptr, make_problem_str
 from ._lib import CxgError, check, lib
 from .problem import QP, Csc
 
+# columns of an iteration-trace row (cxg_batch_trace / cxg_solver_trace)
+TRACE_COLS = 12
+TRACE_NAMES = ["mu", "norm_rx", "norm_rz", "pobj", "dobj", "alpha_aff", "sigma", "alpha", "tau", "kappa", "relres",
+               "attempts"]
+
 
 @dataclass
 class Solution:
@@ -133,6 +138,16 @@ class Solver:
     def solution(self) -> Solution:
         return self._solution
 
+    def trace(self):
+        """Per-iteration trace of the last solve made with record_timings=1: an array of rows with
+        the oracle's trace columns (oracle.TRACE_COLS)."""
+        cap = max(1, self.settings().max_iter)
+        out = np.zeros((cap, TRACE_COLS))
+        k = lib().cxg_solver_trace(self._h, dptr(out), cap)
+        if k < 0:
+            check(k, "cxg_solver_trace")
+        return out[:k]
+
     def backward(self, dl_dx):
         """Adjoint of the last Solved solution: dL/dq, dL/db, dL/d(P values), dL/d(A values)."""
         qp = self._qp
@@ -197,6 +212,15 @@ class BatchSolver:
         check(lib().cxg_batch_solve(self._h, dptr(x), dptr(s), dptr(z),
                                     infos.ctypes.data_as(C.POINTER(Info))), "cxg_batch_solve")
         return x, s, z, infos
+
+    def trace(self, instance):
+        """Per-iteration trace of one instance of the last solve made with record_timings=1."""
+        cap = 1024
+        out = np.zeros((cap, TRACE_COLS))
+        k = lib().cxg_batch_trace(self._h, int(instance), dptr(out), cap)
+        if k < 0:
+            check(k, "cxg_batch_trace")
+        return out[:k]
 
     def backward(self, dl_dx):
         """Adjoint of every instance at its last solution (needs differentiable=1): returns the

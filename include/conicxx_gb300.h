@@ -97,10 +97,17 @@ typedef struct cxg_settings {
                                  device so backward() can reuse them (default 0; cxg_solver: 1);
                                  ignored for whole-GPU roots above 8192 rows */
   int whole_gpu_root;         /* one instance (cxg_solver, or a batch of count 1): 1 = spread the root
-                                 over every SM (cooperative launch, roots up to 64512 rows); -1 =
+                                 over every SM (cooperative launch, roots up to 131072 rows); -1 =
                                  never (one CTA, roots up to 4096 rows); 0 = automatic: cxg_solver
                                  spreads roots of more than 512 rows, a batch of one only roots of
                                  more than 4096 */
+  /* ---- fault injection for tests of the recovery paths (0 = off; counted per instance and
+   *      per solve call, from the start of the solve) ---- */
+  int fault_factor_failures;  /* the first k factorisation attempts report failure, so the x10
+                                 regularisation ladder of factorizeWithRetry runs
+                                 (src/conicxx/kkt/kkt_system.cpp:242-264) */
+  int fault_nonfinite_solves; /* the first k solves with the factor return a non-finite vector, so
+                                 escalateAndResolve's x1000 bumps run (kkt_system.cpp:266-294) */
 } cxg_settings;
 
 /* conicxx::Info (include/conicxx/solution.h:18-26) plus Solution::objective/status and counters. */
@@ -132,6 +139,8 @@ typedef struct cxg_info {
      seconds after the earliest start in the batch (batches; 0 for cxg_solver) */
   double time_start_s;
   double time_end_s;
+  int escalations;            /* refactorisations with x1000 bumps after a non-finite solve
+                                 (escalateAndResolve, src/conicxx/kkt/kkt_system.cpp:266-294) */
 } cxg_info;
 
 /* One problem instance; all pointers are caller-owned host memory (copied, never retained). */
@@ -223,6 +232,8 @@ int cxg_batch_backward_device(cxg_batch* batch, const double* dL_dx, double* dq,
  * - The size buckets run one after another on `stream`, with no captured graph and no stream or
  *   event creation.
  * - Each bucket's persistent grid is cut down to what the array holds.
+ * Like the other solve entry points, it re-orders each bucket's work queue afterwards by the cost
+ * each instance just had (a kernel with static shared memory only).
  *
  * The call allocates nothing. The first call on a device looks up that array's address with the
  * device current. Make that first call before any stream capture.
@@ -247,6 +258,14 @@ int cxg_batch_solve_device_noalloc(cxg_batch* batch, double* x, double* s, doubl
 int cxg_batch_autotune(cxg_batch* batch, int trials, char* report, int reportLen);
 /* Kernel launches enqueued by the last solve/backward call of this batch. */
 int cxg_batch_last_launches(const cxg_batch* batch);
+/* Iteration trace of one instance of the last solve made with record_timings set (no reference
+ * counterpart; the quantities SolverImpl::solve computes per iteration, solver_impl.cpp:367-466):
+ * up to cap_rows rows of 12 doubles each -- mu, ||rx||/tau, ||rz||/tau, primal objective, dual
+ * objective, affine step, sigma, step, tau, kappa, the iteration's largest relative KKT residual,
+ * factorisation attempts. Returns the number of rows written (the instance's iterations, capped),
+ * or a negative CXG_E_* code. */
+int cxg_batch_trace(cxg_batch* batch, int instance, double* out, int cap_rows);
+int cxg_solver_trace(cxg_solver* solver, double* out, int cap_rows);
 /* Device footprint of the batch in bytes: index plans + equilibration (plan), problem values +
  * solutions + results (values), per-CTA working memory (scratch). Any pointer may be NULL. */
 int cxg_batch_footprint(const cxg_batch* batch, int64_t* plan_bytes, int64_t* value_bytes, int64_t* scratch_bytes);

@@ -285,6 +285,8 @@ inline cxg_settings toC(const Settings& s) {
   c.threads_per_instance = s.threads_per_instance;
   c.differentiable = s.differentiable ? 1 : 0;
   c.whole_gpu_root = s.whole_gpu_root;
+  c.fault_factor_failures = 0;
+  c.fault_nonfinite_solves = 0;
   return c;
 }
 }  // namespace detail

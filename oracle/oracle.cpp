@@ -594,6 +594,11 @@ class Ldl {
   // Up-looking numeric factorisation (row k of L from a sparse triangular solve along the
   // elimination tree). QDLDL semantics: an exact zero pivot fails; RegularizedLdlt semantics:
   // correct the pivot, fail if more than 5% were corrected (regularized_ldlt.cpp:107,251).
+  // Attribution: this loop follows the up-looking LDL^T of QDLDL (osqp/qdldl v0.1.9, Copyright
+  // Paul Goulart and Bartolomeo Stellato, Apache License 2.0), which the reference's
+  // src/conicxx/kkt/regularized_ldlt.cpp:166-243 also derives from (its header, :1-23): the
+  // elimination-tree reach into a marker / elimination buffer, then the column updates with a
+  // next-free-slot pointer per column of L.
   bool factor(const Vec& Kx_lower) {
     for (size_t k = 0; k < kmap.size(); ++k) Ux[(size_t)kmap[k]] = Kx_lower[k];
     for (int i = 0; i < N; ++i) {
@@ -826,7 +831,25 @@ class Kkt {
     return factorizeWithRetry();
   }
 
+  // fault injection for tests (cxg_settings::fault_*): armed at the start of every solve
+  int faultFactorLeft = 0, faultSolveLeft = 0;
+  // attempts of factorizeWithRetry and refactorisations of escalateAndResolve since that start
+  int attemptsTotal = 0, escalationsTotal = 0;
+
+  // a solve with the factor; returns a non-finite vector while an injected fault is left
+  void backendSolve(const double* rhs, double* x) {
+    ldl.solve(rhs, x);
+    if (faultSolveLeft > 0) {
+      --faultSolveLeft;
+      x[0] = std::numeric_limits<double>::quiet_NaN();
+    }
+  }
+
   bool tryFactorizeWithBump(double ep, double ea) {
+    if (faultFactorLeft > 0) {
+      --faultFactorLeft;
+      return false;
+    }
     if (ep != 0.0 || ea != 0.0) {
       Vec Kt = Kx;
       if (ep != 0.0)
@@ -845,6 +868,7 @@ class Kkt {
   bool factorizeWithRetry() {
     double ep = 0.0, ea = 0.0;
     for (int attempt = 0; attempt < 18; ++attempt) {
+      ++attemptsTotal;
       if (tryFactorizeWithBump(ep, ea)) {
         factorized = true;
         lastExtraP = ep;
@@ -865,8 +889,9 @@ class Kkt {
     for (int attempt = 0; attempt < 10; ++attempt) {
       ep = std::max(ep * 1000.0, ddelta);
       ea = std::max(ea * 1000.0, ddelta);
+      ++escalationsTotal;
       if (!tryFactorizeWithBump(ep, ea)) continue;
-      ldl.solve(rhs.data(), x.data());
+      backendSolve(rhs.data(), x.data());
       if (allFinite(x)) {
         lastExtraP = ep;
         lastExtraA = ea;
@@ -891,7 +916,7 @@ class Kkt {
   int lastRefineSteps = 0;
   double solve(const Vec& rhs, Vec& x) {
     x.assign((size_t)N, 0.0);
-    ldl.solve(rhs.data(), x.data());
+    backendSolve(rhs.data(), x.data());
     if (!allFinite(x)) escalateAndResolve(rhs, x);
     const double rn = std::max(norm2(rhs.data(), N), 1e-30);
     Vec Kxv((size_t)N), r((size_t)N), dx((size_t)N);
@@ -900,7 +925,7 @@ class Kkt {
     double rel = norm2(r.data(), N) / rn;
     lastRefineSteps = 0;
     for (int it = 0; it < refineMax && rel > refineTol; ++it) {
-      ldl.solve(r.data(), dx.data());
+      backendSolve(r.data(), dx.data());
       for (int i = 0; i < N; ++i) x[(size_t)i] += dx[(size_t)i];
       kmul(x.data(), Kxv.data());
       for (int i = 0; i < N; ++i) r[(size_t)i] = rhs[(size_t)i] - Kxv[(size_t)i];
@@ -1342,6 +1367,10 @@ class Solver {
   void solve() {
     info = cxg_info{};
     trace.clear();
+    kkt.faultFactorLeft = std::max(st.fault_factor_failures, 0);
+    kkt.faultSolveLeft = std::max(st.fault_nonfinite_solves, 0);
+    kkt.attemptsTotal = 0;
+    kkt.escalationsTotal = 0;
     maxRel = 0;
     refineSteps = 0;
     status = CXG_STATUS_UNSOLVED;
@@ -1362,6 +1391,8 @@ class Solver {
       finalize();
       info.status = status;
       info.objective = objective;
+      info.factor_attempts = kkt.attemptsTotal;
+      info.escalations = kkt.escalationsTotal;
       return;
     }
     int fin = CXG_STATUS_MAX_ITERATIONS;
@@ -1444,6 +1475,8 @@ class Solver {
     info.objective = objective;
     info.max_relres = maxRel;
     info.refine_steps = refineSteps;
+    info.factor_attempts = kkt.attemptsTotal;
+    info.escalations = kkt.escalationsTotal;
     if (fin == CXG_STATUS_SOLVED && st.warm_start) {
       wx = x; ws = s; wz = z;
       haveWarm = true;
@@ -1588,8 +1621,18 @@ void orc_cones_scaling(void* h, double* nn_w, double* soc_W, double* soc_Hs) {
 // --- CPU baseline: solve `count` independent instances with `nthreads` threads (one solver
 // per instance, instances handed out by an atomic counter). Setup happens before the timed
 // region. Returns the wall time of the solve phase in seconds.
+double orc_batch_solve_x(int count, const cxg_problem* problems, const cxg_settings* st, int nthreads,
+                         int* statuses, int* iterations, double* x, double* s, double* z);
+
 double orc_batch_solve(int count, const cxg_problem* problems, const cxg_settings* st, int nthreads,
                        int* statuses, int* iterations) {
+  return orc_batch_solve_x(count, problems, st, nthreads, statuses, iterations, nullptr, nullptr, nullptr);
+}
+
+// As orc_batch_solve, and (outside the timed region) the solutions concatenated in instance order
+// into x (sum of n), s and z (sum of m) when those are non-null.
+double orc_batch_solve_x(int count, const cxg_problem* problems, const cxg_settings* st, int nthreads,
+                         int* statuses, int* iterations, double* x, double* s, double* z) {
   std::vector<std::unique_ptr<orc::Solver>> solvers((size_t)count);
   for (int i = 0; i < count; ++i) {
     solvers[(size_t)i] = std::make_unique<orc::Solver>();
@@ -1611,6 +1654,20 @@ double orc_batch_solve(int count, const cxg_problem* problems, const cxg_setting
   for (int t = 0; t < std::max(1, nthreads); ++t) th.emplace_back(work);
   for (auto& t : th) t.join();
   const auto t1 = std::chrono::steady_clock::now();
+  if (x && s && z) {
+    size_t on = 0, om = 0;
+    for (int i = 0; i < count; ++i) {
+      const size_t n = (size_t)problems[i].n, m = (size_t)problems[i].m;
+      const orc::Solver* S = solvers[(size_t)i].get();
+      if (S && S->solx.size() == n && S->sols.size() == m && S->solz.size() == m) {
+        std::memcpy(x + on, S->solx.data(), sizeof(double) * n);
+        std::memcpy(s + om, S->sols.data(), sizeof(double) * m);
+        std::memcpy(z + om, S->solz.data(), sizeof(double) * m);
+      }
+      on += n;
+      om += m;
+    }
+  }
   return std::chrono::duration<double>(t1 - t0).count();
 }
 

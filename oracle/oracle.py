@@ -61,6 +61,9 @@ def lib():
         L.orc_cones_scaling.argtypes = [vp, dp, dp, dp]
         L.orc_batch_solve.argtypes = [C.c_int, C.POINTER(_abi.Problem), C.POINTER(Settings), C.c_int, ip, ip]
         L.orc_batch_solve.restype = C.c_double
+        L.orc_batch_solve_x.argtypes = [C.c_int, C.POINTER(_abi.Problem), C.POINTER(Settings), C.c_int, ip, ip,
+                                        dp, dp, dp]
+        L.orc_batch_solve_x.restype = C.c_double
         _lib = L
     return _lib
 
@@ -240,3 +243,22 @@ def batch_solve(qps, nthreads, settings=None, **kw):
     iters = np.zeros(len(qps), np.int32)
     wall = lib().orc_batch_solve(len(qps), arr, C.byref(st), int(nthreads), iptr(stat), iptr(iters))
     return wall, stat, iters
+
+
+def batch_solve_x(qps, nthreads, settings=None, **kw):
+    """batch_solve plus the concatenated solutions: (wall, statuses, iterations, x, s, z)."""
+    st = settings if settings is not None else default_settings(**kw)
+    structs, keeps = [], []
+    for qp in qps:
+        s_, k = make_problem_struct(qp)
+        structs.append(s_)
+        keeps.append(k)
+    arr = (_abi.Problem * len(qps))(*structs)
+    stat = np.zeros(len(qps), np.int32)
+    iters = np.zeros(len(qps), np.int32)
+    x = np.zeros(sum(q.n for q in qps))
+    s = np.zeros(sum(q.m for q in qps))
+    z = np.zeros(sum(q.m for q in qps))
+    wall = lib().orc_batch_solve_x(len(qps), arr, C.byref(st), int(nthreads), iptr(stat), iptr(iters), dptr(x),
+                                   dptr(s), dptr(z))
+    return wall, stat, iters, x, s, z

@@ -86,3 +86,33 @@ def test_noalloc_rejects_oversized_instance(torch_cuda):
     rc = _noalloc(B, out, infos, torch.cuda.current_stream().cuda_stream)
     assert rc == _abi.E_UNSUPPORTED
     assert b"fixed scratch" in _lib.lib().cxg_last_error()
+
+
+def test_noalloc_grid_cut_to_the_fixed_array(torch_cuda):
+    """512 FP64 contact instances: the largest bucket's persistent grid times its per-CTA working
+    memory exceeds the fixed array, so the entry point runs that bucket on fewer CTAs. Statuses,
+    iterations and x, s, z still equal the regular device solve's."""
+    from conicxx_gb300 import BatchSolver
+
+    torch = torch_cuda
+    qps = generators.contact_batch(512, base_seed=900)
+    B = BatchSolver(qps, warm_start=0, precision=_abi.PRECISION_FP64)
+    cap = (32 << 20) - 256  # CXG_NOALLOC_SCRATCH_BYTES less the queue counters
+    cut = [ln for ln in B.describe().splitlines()
+           if int(ln.split("grid=")[1].split()[0]) * int(ln.split("scratchPerCTA=")[1].split()[0]) * 8 > cap]
+    assert cut, B.describe()  # the grid cut is exercised
+    stream = torch.cuda.current_stream().cuda_stream
+    ref = _buffers(torch, B, 0.0)
+    infos_ref = np.zeros(B.count, dtype=_abi.INFO_DTYPE)
+    B.solve_device(*[t.data_ptr() for t in ref], stream, infos_ref)
+    torch.cuda.synchronize()
+    ref_host = [t.cpu().numpy() for t in ref]
+    out = _buffers(torch, B, float("nan"))
+    infos = np.zeros(B.count, dtype=_abi.INFO_DTYPE)
+    rc = _noalloc(B, out, infos, stream)
+    assert rc == _abi.OK, _lib.lib().cxg_last_error()
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(infos["status"], infos_ref["status"])
+    np.testing.assert_array_equal(infos["iterations"], infos_ref["iterations"])
+    for name, got, want in zip("xsz", out, ref_host):
+        assert rel(got.cpu().numpy(), want) < SOL_TOL, name
