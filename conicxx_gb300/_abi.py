@@ -58,6 +58,7 @@ class Settings(C.Structure):
         ("whole_gpu_root", C.c_int),
         ("fault_factor_failures", C.c_int),
         ("fault_nonfinite_solves", C.c_int),
+        ("soc_reference_dense", C.c_int),
     ]
 
 
@@ -71,7 +72,7 @@ def default_settings(**overrides):
         warm_start=1, verbose=0, record_timings=0, validate_inputs=1,
         linear_solver=LINSOLVER_QDLDL, precision=PRECISION_FP64, mixed_refine_max_iter=4,
         mixed_fallback_tol=1e-10, threads_per_instance=0, differentiable=0,
-        whole_gpu_root=0, fault_factor_failures=0, fault_nonfinite_solves=0,
+        whole_gpu_root=0, fault_factor_failures=0, fault_nonfinite_solves=0, soc_reference_dense=1,
     )
     for k, v in overrides.items():
         if not hasattr(s, k):

@@ -100,6 +100,7 @@ extern "C" void cxg_default_settings(cxg_settings* s) {
   s->whole_gpu_root = 0;
   s->fault_factor_failures = 0;
   s->fault_nonfinite_solves = 0;
+  s->soc_reference_dense = 1;
 }
 
 // ------------------------------------------------------------------------------------------
@@ -194,6 +195,7 @@ static DevSettings makeDevSettings(const cxg_settings& st, const cxg_settings& k
   d.record_timings = st.record_timings ? 1 : 0;
   d.fault_factor_failures = std::max(st.fault_factor_failures, 0);
   d.fault_nonfinite_solves = std::max(st.fault_nonfinite_solves, 0);
+  d.soc_ref_dense = kk.soc_reference_dense ? 1 : 0;
   return d;
 }
 
@@ -223,7 +225,8 @@ static const int kGridAutoRoot = 512;
 static const int kGridMaxRoot = 131072;
 static const int kGridMaxAdjointRoot = 8192;
 // shared memory of the whole-GPU trailing update (8-byte entries; see gridStageBytes)
-static const int64_t kGridStageBytes = (2ll * kTile * 128 + 16ll * kTileElems) * 8;
+// (8-byte entries; see gridStageBytes), or the FP32 tensor-core update's, whichever is larger
+static const int64_t kGridStageBytes = std::max<int64_t>((2ll * kTile * 128 + 16ll * kTileElems) * 8, kGridTcStageBytes);
 
 static int chooseBlock(int nrMax, int requested) {
   if (requested == 32 || requested == 64 || requested == 128 || requested == 256) return requested;

@@ -24,9 +24,13 @@ constexpr double kTinyRel = 1e-12;                 // second_order_cone.cpp:89
 constexpr double kAbsFloor = kDblMin * 1e4;        // second_order_cone.cpp:90
 constexpr double kBetaMax = 1e8;                   // second_order_cone.cpp:106
 constexpr double kWMax = 1e8;                      // second_order_cone.cpp:152
+// relative resolution of a dense FP64 Hs = W W (one ulp of its largest eigenvalue); see the
+// reference dense form below
+constexpr double kHsRes = 2.220446049250313e-16;
 
 // Per-SOC-block scaling parameters (8 doubles in shared memory):
-// [0] kind (0 identity fallback, 1 diagonal, 2 plane), [1] beta, [2] lambda (plane) or
+// [0] kind (0 identity fallback, 1 diagonal, 2 plane, 3 plane with the small eigenvalue of Hs held
+// at the dense form's resolution, hsSmall), [1] beta, [2] lambda (plane) or
 // a = 2v0^2-1 (diagonal), [3] q1c, [4] q1s (in-plane eigenvector of lambda), [5..7] the three
 // eigenvalues of G = (Hs + eps I)^-1 prepared at factorisation time (socPrepareG).
 // The unit vector u is kept in a row-indexed array at rows off+1 .. off+dim-1.
@@ -121,6 +125,18 @@ __device__ __forceinline__ double wfun(int f, double w, double eps) {
   }
 }
 
+// Functions of Hs given one of its eigenvalues h (f = kHs, kHsEps, kGinv).
+__device__ __forceinline__ double hsfun(int f, double h, double eps) {
+  return f == kHs ? h : (f == kHsEps ? h + eps : 1.0 / (h + eps));
+}
+
+// The small in-plane eigenvalue of Hs of a kind-3 block: (beta / lambda)^2, held at no less than
+// kHsRes (beta lambda)^2.
+__device__ __forceinline__ double hsSmall(const SocScale& sc) {
+  const double w1 = sc.beta * sc.lam, w2 = sc.beta / sc.lam;
+  return fmax(w2 * w2, kHsRes * (w1 * w1));
+}
+
 // y = f(W) x for one SOC block (x, y may alias only if identical).
 __device__ __forceinline__ void socApply(const SocScale& sc, const double* u, int d, int f, double eps,
                                          const double* x, double* y) {
@@ -143,7 +159,7 @@ __device__ __forceinline__ void socApply(const SocScale& sc, const double* u, in
   const double c1 = sc.qc * x0 + sc.qs * xf;
   const double c2 = -sc.qs * x0 + sc.qc * xf;
   const double f1 = wfun(f, sc.beta * sc.lam, eps);
-  const double f2 = wfun(f, sc.beta / sc.lam, eps);
+  const double f2 = (kind == 3 && f >= kHs) ? hsfun(f, hsSmall(sc), eps) : wfun(f, sc.beta / sc.lam, eps);
   const double f3 = wfun(f, sc.beta, eps);
   const double y0 = f1 * c1 * sc.qc - f2 * c2 * sc.qs;
   const double yF = f1 * c1 * sc.qs + f2 * c2 * sc.qc;
@@ -164,7 +180,7 @@ __device__ __forceinline__ void socPrepareG(SocScale& sc, double eps) {
   } else {
     const double w1 = sc.beta * sc.lam, w2 = sc.beta / sc.lam, w3 = sc.beta;
     sc.r0 = 1.0 / (w1 * w1 + eps);
-    sc.r1 = 1.0 / (w2 * w2 + eps);
+    sc.r1 = 1.0 / ((kind == 3 ? hsSmall(sc) : w2 * w2) + eps);
     sc.r2 = 1.0 / (w3 * w3 + eps);
   }
 }
@@ -253,6 +269,121 @@ __device__ __forceinline__ double socMaxStep(const double* x, const double* dx, 
   if (r1 > 0 && (p0 + r1 * d0) >= 0) alpha = fmin(alpha, r1);
   if (r2 > 0 && (p0 + r2 * d0) >= 0) alpha = fmin(alpha, r2);
   return alpha;
+}
+
+// ---- a second-order block in the reference's dense FP64 form -----------------------------
+// The reference keeps a block's Hs = W W as a dense FP64 matrix, W = beta (2 v v' - J) formed
+// entry by entry (second_order_cone.cpp:132-158). Near the cone boundary the in-plane eigenvalues
+// of Hs, beta^2 lambda^2 and beta^2 / lambda^2, lie more than 1/eps_machine apart, and the dense
+// entries no longer carry the small one: it is replaced by rounding of the order of
+// eps_machine * beta^2 lambda^2. The eigen-form held here is exact to rounding. Two of the
+// reference's decisions depend on that rounding, and both are reproduced from the dense entries
+// in the reference's arithmetic (its operation order, no fused multiply-adds) for blocks of up to
+// kRefDenseMaxDim rows:
+//  - the sparse LDL' of K (qdldl_ldlt.cpp:58-69) takes a block's rows before the x rows they
+//    couple to (a block row has degree dim - 1 + the nonzeros of its A row), so the block
+//    -(Hs + eps I) is factored on its own; its last pivot comes out zero or below
+//    dynamic_reg_eps and factorizeWithRetry (kkt_system.cpp:242-264) fails the attempt and raises
+//    the bump x10 until the bump survives the block's rounding (socRefLadderLevel);
+//  - Hs itself: from the first iteration in which that pivot test fails, the instance holds the
+//    small in-plane eigenvalue of Hs at no less than kHsRes times the large one (kind 3 in
+//    SocScale: Hs, Hs + eps I and G; W and W^-1 stay exact), the resolution of the dense form.
+//    With the exact small eigenvalue the iteration drives the complementarity of such blocks to
+//    zero ahead of primal feasibility and then stalls (configuration 2's family from 3000
+//    variables on; the reference's own iteration with exact Hs products slows from 26 to 76
+//    iterations there); at the dense form's resolution it converges as the reference does.
+constexpr int kRefDenseMaxDim = 8;
+constexpr int kLadderLevels = 18;  // factorizeWithRetry's attempts (kkt_system.cpp:242-264)
+
+// the bump of ladder attempt `level`: 0, delta, 10 delta, ... (kkt_system.cpp:258-259)
+__host__ __device__ __forceinline__ double ladderBump(int level, double delta) {
+  double e = 0.0;
+  for (int k = 0; k < level; ++k) e = fmax(e * 10.0, delta);
+  return e;
+}
+
+// Dense Hs of one block (row-major d x d, d <= kRefDenseMaxDim) in the reference's arithmetic;
+// false for the identity fallback (W non-finite or max |W_ij| > 1e8), where Hs = I.
+static __device__ __noinline__ bool socRefHs(const double* s, const double* z, int d, double* Hs) {
+  double v[kRefDenseMaxDim];
+  double s1sq = 0.0, z1sq = 0.0, sz = 0.0;
+  for (int i = 1; i < d; ++i) {
+    s1sq = __dadd_rn(s1sq, __dmul_rn(s[i], s[i]));
+    z1sq = __dadd_rn(z1sq, __dmul_rn(z[i], z[i]));
+  }
+  for (int i = 0; i < d; ++i) sz = __dadd_rn(sz, __dmul_rn(s[i], z[i]));
+  const double s0 = s[0], z0 = z[0];
+  const double a =
+      __dsqrt_rn(fmax(fmax(__dsub_rn(__dmul_rn(s0, s0), s1sq), __dmul_rn(__dmul_rn(kTinyRel, s0), s0)), kAbsFloor));
+  const double b =
+      __dsqrt_rn(fmax(fmax(__dsub_rn(__dmul_rn(z0, z0), z1sq), __dmul_rn(__dmul_rn(kTinyRel, z0), z0)), kAbsFloor));
+  const double beta = fmin(fmax(__dsqrt_rn(__ddiv_rn(a, b)), __ddiv_rn(1.0, kBetaMax)), kBetaMax);
+  const double c = __dsqrt_rn(fmax(__ddiv_rn(__dadd_rn(__ddiv_rn(sz, __dmul_rn(a, b)), 1.0), 2.0), kTiny));
+  v[0] = __dadd_rn(__ddiv_rn(z0, b), __ddiv_rn(s0, a));
+  for (int i = 1; i < d; ++i) v[i] = __dadd_rn(__ddiv_rn(-z[i], b), __ddiv_rn(s[i], a));
+  const double c2 = __dmul_rn(2.0, c);
+  for (int i = 0; i < d; ++i) v[i] = __ddiv_rn(v[i], c2);
+  v[0] = fmax(__dadd_rn(v[0], 1.0), kTiny);
+  const double nrm = __dsqrt_rn(__dmul_rn(2.0, v[0]));
+  for (int i = 0; i < d; ++i) v[i] = __ddiv_rn(v[i], nrm);
+  auto W = [&](int r, int cc) {
+    double w = __dmul_rn(__dmul_rn(2.0, v[r]), v[cc]);
+    if (r == cc) w = (r == 0) ? __dsub_rn(w, 1.0) : __dadd_rn(w, 1.0);
+    return __dmul_rn(w, beta);
+  };
+  double wmax = 0.0;
+  bool finite = true;
+  for (int r = 0; r < d; ++r)
+    for (int cc = 0; cc < d; ++cc) {
+      const double w = W(r, cc);
+      finite = finite && isfinite(w);
+      wmax = fmax(wmax, fabs(w));
+    }
+  if (finite && wmax <= kWMax) {
+    for (int r = 0; r < d; ++r)
+      for (int cc = 0; cc < d; ++cc) {
+        double acc = 0.0;
+        for (int k = 0; k < d; ++k) acc = __dadd_rn(acc, __dmul_rn(W(r, k), W(k, cc)));
+        finite = finite && isfinite(acc);
+        Hs[r * d + cc] = acc;
+      }
+    if (finite) return true;
+  }
+  for (int r = 0; r < d; ++r)
+    for (int cc = 0; cc < d; ++cc) Hs[r * d + cc] = (r == cc) ? 1.0 : 0.0;
+  return false;
+}
+
+// The first ladder level (attempt index, 0..17) at which the block's dense pivots all pass, or
+// 18 when none does; the search starts at startLevel (a block that passes there returns
+// startLevel). Blocks of one row or above kRefDenseMaxDim rows: 0.
+static __device__ __noinline__ int socRefLadderLevel(const double* s, const double* z, int d, double sregA,
+                                                     double deps, double delta, int startLevel) {
+  if (d > kRefDenseMaxDim || d < 2) return 0;
+  double Hs[kRefDenseMaxDim * kRefDenseMaxDim];
+  if (!socRefHs(s, z, d, Hs)) return 0;  // Hs = I: every pivot passes
+  for (int level = startLevel; level < kLadderLevels; ++level) {
+    const double ea = ladderBump(level, delta);
+    // up-looking LDL' of -(Hs + sregA I) - ea I in natural order, QDLDL's operation order
+    double L[kRefDenseMaxDim * kRefDenseMaxDim], Dinv[kRefDenseMaxDim], y[kRefDenseMaxDim];
+    bool ok = true;
+    for (int k = 0; k < d && ok; ++k) {
+      double Dk = __dsub_rn(-Hs[k * d + k], sregA);
+      if (ea != 0.0) Dk = __dsub_rn(Dk, ea);
+      for (int r = 0; r < k; ++r) y[r] = -Hs[k * d + r];
+      for (int cc = 0; cc < k; ++cc) {
+        const double yc = y[cc];
+        for (int r = cc + 1; r < k; ++r) y[r] = __dsub_rn(y[r], __dmul_rn(L[r * kRefDenseMaxDim + cc], yc));
+        const double l = __dmul_rn(yc, Dinv[cc]);
+        L[k * kRefDenseMaxDim + cc] = l;
+        Dk = __dsub_rn(Dk, __dmul_rn(yc, l));
+      }
+      ok = isfinite(Dk) && fabs(Dk) > deps;
+      Dinv[k] = __ddiv_rn(1.0, Dk);
+    }
+    if (ok) return level;
+  }
+  return kLadderLevels;
 }
 
 __device__ __forceinline__ double socMargin(const double* x, int d) {

@@ -23,6 +23,7 @@
 #include "cxg_df64.cuh"
 #include "cxg_kernels.h"
 #include "cxg_layout.h"
+#include "cxg_tc.cuh"
 
 namespace cxg {
 
@@ -114,6 +115,15 @@ __device__ __forceinline__ int blockOrInt(int v, int* redi) {
   return redi[0];
 }
 
+__device__ __forceinline__ int blockMaxInt(int v, int* redi) {
+  __syncthreads();
+  if (threadIdx.x == 0) redi[0] = 0;
+  __syncthreads();
+  if (v) atomicMax(redi, v);
+  __syncthreads();
+  return redi[0];
+}
+
 // ------------------------------------------------------------------------------------------
 // per-instance context (pointers into shared memory, scratch and the pools)
 // ------------------------------------------------------------------------------------------
@@ -142,8 +152,10 @@ struct Ctx {
 // scalar slots in Ctx::sc
 enum {
   SC_TAU = 0, SC_KAPPA, SC_EXTRA_P, SC_EXTRA_A, SC_USE64, SC_NFB, SC_RSTEPS, SC_MAXREL,
-  SC_ATTEMPTS, SC_FACTOK, SC_GMRES, SC_ITREL, SC_FAULTF, SC_FAULTS, SC_ESC, SC_COUNT
+  SC_ATTEMPTS, SC_FACTOK, SC_GMRES, SC_ITREL, SC_FAULTF, SC_FAULTS, SC_ESC, SC_SOCLVL, SC_HSFLOOR, SC_COUNT
 };
+
+
 
 // Phase cycle counters (record_timings), kept by thread 0 in the scalar area after PivotStats.
 enum { TM_FACTOR = 0, TM_SOLVE = 1, TM_ASSEMBLE = 2, TM_LDLT = 3, TM_DSOLVE = 4, TM_RESID = 5, TM_COUNT = 6 };
@@ -188,7 +200,13 @@ static __device__ __noinline__ void loadInstance(Ctx& c, const LaunchArgs& a) {
 // ------------------------------------------------------------------------------------------
 // cone-set operations over all units of the instance (cone_set.cpp)
 // ------------------------------------------------------------------------------------------
-static __device__ __noinline__ void coneUpdateScaling(Ctx& c, const double* s, const double* z) {
+// Also leaves in c.sc[SC_SOCLVL] the first attempt of the regularisation ladder at which every SOC
+// block's dense pivots pass in the reference's arithmetic (socRefLadderLevel; 0 when the test is
+// off): the earlier attempts of factorizeWithRetry fail as the reference's do. From the first
+// iteration with such a failure on, the instance's blocks hold Hs at the dense form's resolution
+// (kind 3, hsSmall; flag SC_HSFLOOR).
+static __device__ __noinline__ void coneUpdateScaling(Ctx& c, const DevSettings& st, const double* s, const double* z) {
+  int lvl = 0;
   FOR_T(t, c.l + c.nsoc) {
     if (t < c.l) {
       const int r = c.p + t;
@@ -197,7 +215,20 @@ static __device__ __noinline__ void coneUpdateScaling(Ctx& c, const double* s, c
       const int b = t - c.l;
       const int off = c.socOff[b], d = c.socDim[b];
       socUpdateScaling(s + off, z + off, d, c.sp[b], c.cu + off);
+      if (st.soc_ref_dense && st.linear_solver != 2)
+        lvl = max(lvl, socRefLadderLevel(s + off, z + off, d, st.static_reg_A, st.dynamic_reg_eps,
+                                         st.dynamic_reg_delta, lvl));
     }
+  }
+  const int mx = blockMaxInt(lvl, c.redi);
+  // once a block's dense form has lost its small eigenvalue (the reference's pivot test fails),
+  // the instance's blocks take Hs at the dense form's resolution, from this iteration on (sticky)
+  const bool floorHs = c.sc[SC_HSFLOOR] != 0.0 || mx > 0;
+  if (floorHs) FOR_T(b, c.nsoc) if (c.sp[b].kind == 2.0) c.sp[b].kind = 3.0;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    c.sc[SC_SOCLVL] = (double)mx;
+    if (floorHs) c.sc[SC_HSFLOOR] = 1.0;
   }
   __syncthreads();
 }
@@ -1241,6 +1272,183 @@ __device__ __noinline__ void superSyrk(T* M, int Tn, int J, int I0, int K0, int 
   }
 }
 
+// FP32 trailing update of tile column J on the tensor cores (tcgen05, kind::tf32): the same
+// C_IK -= L_IJ D_J L_KJ^T as superSyrk, over every super-block this CTA owns in the step
+// (sb = blockIdx.x - 1, + gridDim.x - 1, ...). Each FP32 operand is split as hi + lo (hi = its
+// TF32 rounding, lo = the TF32 rounding of the remainder) and the product taken as
+// A_lo B_hi + A_hi B_lo + A_hi B_hi (3xTF32; the A_lo B_lo term is below FP32 rounding): twelve
+// 128x128x8 MMAs accumulating in FP32 in TMEM, issued by one thread. Software pipeline: the C tiles
+// of the next super-block arrive by bulk copies (TMA) into the other of two shared-memory buffers
+// while the current super-block's panels are staged (generic loads, TF32 split), multiplied and
+// its tiles updated from TMEM and written back by bulk copies. All bulk stores of the step are
+// complete (and ordered before later generic accesses) when it returns.
+// Shared memory `sm` (128-byte aligned, kGridTcStageBytes): the operand panels A_hi, A_lo, B_hi,
+// B_lo (16 KB each, layout of cxg_tc.cuh), then two buffers of 16 C tiles. `tmem`: this CTA's 128
+// accumulator columns; mbarriers: MMA completion and one per C buffer, with their phase parities.
+// Returns false when a wait ran out (after waiting once more for the copies in flight).
+constexpr int64_t kTcStageBytes = kGridTcStageBytes;
+constexpr unsigned long long kTcWaitNs = 2ull * 1000ull * 1000ull * 1000ull;
+constexpr uint32_t kTileBytes = (uint32_t)kTileElems * 4u;
+
+struct SbGeo {
+  int I0, K0, ni, nk;
+  bool diag, skip00;
+};
+
+// the super-block sb of step J (row order: sb = r (r + 1) / 2 + k, tile rows J+1+4r.., tile
+// columns J+1+4k..; super-block 0 without the tile (J+1, J+1), which CTA 0 updates)
+__device__ __forceinline__ SbGeo sbGeo(long long sb, int J, int Tn) {
+  int r = (int)((sqrtf(8.0f * (float)sb + 1.0f) - 1.0f) * 0.5f);
+  while ((long long)r * (r + 1) / 2 > sb) --r;
+  while ((long long)(r + 1) * (r + 2) / 2 <= sb) ++r;
+  const int k = (int)(sb - (long long)r * (r + 1) / 2);
+  SbGeo g;
+  g.I0 = J + 1 + 4 * r;
+  g.K0 = J + 1 + 4 * k;
+  g.ni = min(4, Tn - g.I0);
+  g.nk = min(4, Tn - g.K0);
+  g.diag = r == k;
+  g.skip00 = sb == 0;
+  return g;
+}
+
+// tile t = 4a + b of the super-block is updated (and so loaded and stored) by it
+__device__ __forceinline__ bool sbTile(const SbGeo& g, int t) {
+  const int a = t >> 2, b = t & 3;
+  return a < g.ni && b < g.nk && !(g.diag && b > a) && !(g.skip00 && t == 0);
+}
+
+static __device__ __noinline__ bool tcTrailingStep(float* M, int Tn, int J, long long nsb, unsigned char* sm,
+                                                   uint32_t tmem, uint32_t mbarMma, uint32_t mbarLd0,
+                                                   uint32_t mbarLd1, uint32_t& phMma, uint32_t& phLd0,
+                                                   uint32_t& phLd1) {
+  const int tid = threadIdx.x;
+  const long long first = (long long)blockIdx.x - 1, stride = (long long)gridDim.x - 1;
+  if (first >= nsb) return true;
+  const float* Ajj = M + tileBase(Tn, J, J);
+  const uint32_t opBase = tc::smemAddr(sm);
+  const uint32_t cAddr[2] = {opBase + 4u * tc::kPanelBytes, opBase + 4u * tc::kPanelBytes + 16u * kTileBytes};
+  float* cPtr[2] = {reinterpret_cast<float*>(sm + 4 * tc::kPanelBytes),
+                    reinterpret_cast<float*>(sm + 4 * tc::kPanelBytes + 16 * kTileBytes)};
+  const uint32_t mbarLd[2] = {mbarLd0, mbarLd1};
+  // thread 0: the C tiles of super-block g into buffer buf, completing on that buffer's mbarrier
+  auto issueLoads = [&](const SbGeo& g, int buf) {
+    uint32_t bytes = 0;
+    for (int t = 0; t < 16; ++t)
+      if (sbTile(g, t)) bytes += kTileBytes;
+    tc::mbarArriveExpectTx(mbarLd[buf], bytes);
+    for (int t = 0; t < 16; ++t)
+      if (sbTile(g, t))
+        tc::bulkLoad(cAddr[buf] + (uint32_t)t * kTileBytes, M + tileBase(Tn, g.I0 + (t >> 2), g.K0 + (t & 3)),
+                     kTileBytes, mbarLd[buf]);
+  };
+  if (tid == 0) {
+    tc::fenceProxyAsyncGlobal();  // the previous step's generic writes before these async reads
+    issueLoads(sbGeo(first, J, Tn), 0);
+  }
+  int buf = 0;
+  for (long long sb = first; sb < nsb; sb += stride, buf ^= 1) {
+    const SbGeo g = sbGeo(sb, J, Tn);
+    if (tid == 0 && sb + stride < nsb) {
+      tc::bulkWaitRead0();  // the previous super-block's stores have read the other buffer
+      issueLoads(sbGeo(sb + stride, J, Tn), buf ^ 1);
+    }
+    // panels: thread tid stages row i = tid & 127 of A (L_IJ, tid < 128) or of B (D-scaled L_KJ),
+    // four k at a time, as TF32 hi and lo parts; row m sits at byte (k / 4) * 2048 + m * 16 + (k % 4) * 4
+    if (tid < 2 * tc::kRows) {
+      const int i = tid & (tc::kRows - 1), isB = tid >> 7, a = i >> 5, rr = i & 31;
+      const int nt = isB ? g.nk : g.ni;
+      const float* src = (a < nt) ? M + tileBase(Tn, (isB ? g.K0 : g.I0) + a, J) + rr : nullptr;
+      unsigned char* hiBase = sm + (isB ? 2 : 0) * tc::kPanelBytes;
+      unsigned char* loBase = hiBase + tc::kPanelBytes;
+#pragma unroll 2
+      for (int kq = 0; kq < kTile / 4; ++kq) {
+        float hi[4], lo[4];
+#pragma unroll
+        for (int t = 0; t < 4; ++t) {
+          const int k = 4 * kq + t;
+          float x = src ? src[k * kTileLd] : 0.0f;
+          if (isB) x = x * Ajj[k * kTileLd + k];
+          hi[t] = tc::toTf32(x);
+          lo[t] = tc::toTf32(x - hi[t]);
+        }
+        *reinterpret_cast<float4*>(hiBase + kq * 2048 + i * 16) = make_float4(hi[0], hi[1], hi[2], hi[3]);
+        *reinterpret_cast<float4*>(loBase + kq * 2048 + i * 16) = make_float4(lo[0], lo[1], lo[2], lo[3]);
+      }
+    }
+    tc::fenceProxyAsyncShared();
+    __syncthreads();
+    if (tid == 0) {
+      tc::fenceAfterSync();
+      const uint32_t aHi = opBase, aLo = opBase + tc::kPanelBytes, bHi = opBase + 2 * tc::kPanelBytes,
+                     bLo = opBase + 3 * tc::kPanelBytes;
+      constexpr uint32_t idesc = tc::idescTf32(tc::kRows, tc::kRows);
+      for (int sK = 0; sK < kTile / 8; ++sK) {
+        const uint32_t o = (uint32_t)sK * 4096u;
+        tc::mmaTf32(tmem, tc::smemDesc(aLo + o), tc::smemDesc(bHi + o), idesc, sK > 0);
+        tc::mmaTf32(tmem, tc::smemDesc(aHi + o), tc::smemDesc(bLo + o), idesc, true);
+      }
+      for (int sK = 0; sK < kTile / 8; ++sK) {
+        const uint32_t o = (uint32_t)sK * 4096u;
+        tc::mmaTf32(tmem, tc::smemDesc(aHi + o), tc::smemDesc(bHi + o), idesc, true);
+      }
+      tc::commitTo(mbarMma);
+    }
+    // the product and this buffer's C tiles (bounded waits; one vote for the whole CTA)
+    uint32_t& phLd = buf ? phLd1 : phLd0;
+    bool ok = tc::mbarWait(mbarMma, phMma, kTcWaitNs);
+    ok = tc::mbarWait(mbarLd[buf], phLd, kTcWaitNs) && ok;
+    phMma ^= 1u;
+    phLd ^= 1u;
+    tc::fenceAfterSync();
+    if (!__syncthreads_and(ok)) {
+      // a wait ran out: give the copies and MMAs in flight one more period, then give up
+      tc::mbarWait(mbarMma, phMma ^ 1u, kTcWaitNs);
+      tc::mbarWait(mbarLd[buf ^ 1], buf ? phLd0 : phLd1, kTcWaitNs);
+      if (tid == 0) tc::bulkWait0();
+      __syncthreads();
+      return false;
+    }
+    // C -= product: warp w reads TMEM lanes 32 (w % 4) .. +31 (its rows), columns 64 (w / 4) ..
+    // +63, sixteen at a time
+    {
+      float* Cs = cPtr[buf];
+      const int warp = tid >> 5, lane = tid & 31;
+      if (warp < 8) {
+        const int q = warp & 3, h = warp >> 2;
+        const int R = 32 * q + lane;
+        for (int cb = 0; cb < 4; ++cb) {
+          float d[16];
+          const int c0 = 64 * h + 16 * cb;
+          tc::tmemLoad16(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)c0, d);
+#pragma unroll
+          for (int j = 0; j < 16; ++j) {
+            const int Cc = c0 + j;
+            float& cref = Cs[((R >> 5) * 4 + (Cc >> 5)) * kTileElems + (Cc & 31) * kTileLd + (R & 31)];
+            cref = cref - d[j];
+          }
+        }
+      }
+    }
+    tc::fenceProxyAsyncShared();  // the updated tiles visible to the bulk stores
+    tc::fenceBeforeSync();
+    __syncthreads();
+    if (tid == 0) {
+      for (int t = 0; t < 16; ++t)
+        if (sbTile(g, t))
+          tc::bulkStore(M + tileBase(Tn, g.I0 + (t >> 2), g.K0 + (t & 3)), cAddr[buf] + (uint32_t)t * kTileBytes,
+                        kTileBytes);
+      tc::bulkCommit();
+    }
+  }
+  if (tid == 0) {
+    tc::bulkWait0();
+    tc::fenceProxyAsyncGlobal();  // the stores before the grid barrier's generic release
+  }
+  __syncthreads();
+  return true;
+}
+
 // Tiled right-looking LDL' of the root over the whole grid. Per tile column J:
 //  (A) the off-diagonal tiles of column J, one warp each; barrier;
 //  (B) the trailing update C_IK -= L_IJ D_J L_KJ^T, J < K <= I, in super-blocks of 4x4 tiles, one
@@ -1249,12 +1457,54 @@ __device__ __noinline__ void superSyrk(T* M, int Tn, int J, int I0, int K0, int 
 // Every root entry receives its updates in increasing J with the same operations and rounding as
 // the single-CTA factor, so both give the same bits. Only warp 0 of CTA 0 factors diagonal tiles,
 // so the pivot statistics stay in CTA 0's shared memory (ps). `stage` holds gridStageBytes.
+// tensor-core state of a CTA for the length of one factorisation job
+struct TcState {
+  unsigned char* stage;  // kGridTcStageBytes, 128-byte aligned
+  uint32_t tmem, mbar;   // TMEM base; three mbarriers at mbar, mbar + 8, mbar + 16
+  uint32_t phMma, phLd0, phLd1;
+};
+
+template <typename T>
+__device__ __noinline__ bool gridLdltSteps(GridCtl* g, int nr, int nx, const DevSettings& st, T* M, PivotStats* ps,
+                                           T* stage, int Tn, int warp, int gw, int GW, bool cta0, TcState& tcs);
+
 template <typename T>
 __device__ __noinline__ bool gridLdlt(GridCtl* g, int nr, int nx, const DevSettings& st, T* M, PivotStats* ps, T* stage) {
   const int Tn = rootTiles(nr);
   const int warp = threadIdx.x >> 5, W = blockDim.x >> 5;
   const int gw = (int)blockIdx.x * W + warp, GW = (int)gridDim.x * W;
   const bool cta0 = blockIdx.x == 0;
+  // FP32: the super-blocks go to the tensor cores; every CTA but 0 holds 128 TMEM columns and an
+  // mbarrier for the length of the job
+  constexpr bool kTc = sizeof(T) == 4;
+  __shared__ __align__(8) unsigned long long sMbar[3];  // MMA completion, C buffer 0, C buffer 1
+  __shared__ uint32_t sTmem;
+  TcState tcs{};
+  tcs.mbar = tc::smemAddr(&sMbar[0]);
+  tcs.stage = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(stage) + 127) & ~static_cast<uintptr_t>(127));
+  if (kTc && !cta0) {
+    if (warp == 0) tc::tmemAlloc(tc::smemAddr(&sTmem), tc::kTmemCols);
+    if (threadIdx.x == 32)
+      for (int i = 0; i < 3; ++i) tc::mbarInit(tcs.mbar + 8u * i, 1);
+    tc::fenceBeforeSync();
+    __syncthreads();
+    tc::fenceAfterSync();
+    tcs.tmem = sTmem;
+  }
+  const bool ok = gridLdltSteps<T>(g, nr, nx, st, M, ps, stage, Tn, warp, gw, GW, cta0, tcs);
+  if (kTc && !cta0) {
+    tc::fenceBeforeSync();
+    __syncthreads();
+    if (warp == 0) tc::tmemDealloc(tcs.tmem, tc::kTmemCols);
+    if (threadIdx.x == 32)
+      for (int i = 0; i < 3; ++i) tc::mbarInval(tcs.mbar + 8u * i);
+  }
+  return ok;
+}
+
+template <typename T>
+__device__ __noinline__ bool gridLdltSteps(GridCtl* g, int nr, int nx, const DevSettings& st, T* M, PivotStats* ps,
+                                           T* stage, int Tn, int warp, int gw, int GW, bool cta0, TcState& tcs) {
   if (cta0 && warp == 0) tileFactorDiag<T>(M, 0, nr, nx, st, ps);
   if (!gridSync(g)) return false;
   for (int J = 0; J + 1 < Tn; ++J) {
@@ -1277,14 +1527,18 @@ __device__ __noinline__ bool gridLdlt(GridCtl* g, int nr, int nx, const DevSetti
       if (!gridSync(g)) return false;
       continue;
     }
-    for (long long sb = (long long)blockIdx.x - 1; sb < nsb; sb += (long long)gridDim.x - 1) {
-      int r = (int)((sqrtf(8.0f * (float)sb + 1.0f) - 1.0f) * 0.5f);
-      while ((long long)r * (r + 1) / 2 > sb) --r;
-      while ((long long)(r + 1) * (r + 2) / 2 <= sb) ++r;
-      const int k = (int)(sb - (long long)r * (r + 1) / 2);
-      const int I0 = J + 1 + 4 * r, K0 = J + 1 + 4 * k;
-      __syncthreads();  // the previous super-block is done with the staging area
-      superSyrk<T>(M, Tn, J, I0, K0, min(4, Tn - I0), min(4, Tn - K0), r == k, sb == 0, stage);
+    if constexpr (sizeof(T) == 4) {
+      if (!tcTrailingStep(M, Tn, J, nsb, tcs.stage, tcs.tmem, tcs.mbar, tcs.mbar + 8u, tcs.mbar + 16u, tcs.phMma,
+                          tcs.phLd0, tcs.phLd1)) {
+        if (threadIdx.x == 0) atomicExch(&g->error, 1);
+        return false;
+      }
+    } else {
+      for (long long sb = (long long)blockIdx.x - 1; sb < nsb; sb += (long long)gridDim.x - 1) {
+        const SbGeo gg = sbGeo(sb, J, Tn);
+        __syncthreads();  // the previous super-block is done with the staging area
+        superSyrk<T>(M, Tn, J, gg.I0, gg.K0, gg.ni, gg.nk, gg.diag, gg.skip00, stage);
+      }
     }
     if (!gridSync(g)) return false;
   }
@@ -1680,9 +1934,25 @@ __device__ __forceinline__ typename HighT<FT>::type* rootHigh(Ctx& c) {
 template <typename FT, bool G = false>
 __device__ __noinline__ bool factorizeWithRetryImpl(Ctx& c, const DevSettings& st, FactState& fs) {
   double ep = 0.0, ea = 0.0;
+  // attempts below this level fail in the reference's dense SOC blocks (coneUpdateScaling)
+  const int socLvl = (int)c.sc[SC_SOCLVL];
   for (int attempt = 0; attempt < 18; ++attempt) {
     int fail = 0, wrong = 0;
     double mind = 0.0;
+    // fault injection (tests): this attempt reports failure before any work, as does an attempt
+    // the reference's SOC-block pivots fail
+    const bool injected = c.sc[SC_FAULTF] < (double)st.fault_factor_failures;
+    __syncthreads();
+    if (injected || attempt < socLvl) {
+      if (threadIdx.x == 0) {
+        c.sc[SC_ATTEMPTS] += 1.0;
+        if (injected) c.sc[SC_FAULTF] += 1.0;
+      }
+      __syncthreads();
+      ep = fmax(ep * 10.0, st.dynamic_reg_delta);
+      ea = fmax(ea * 10.0, st.dynamic_reg_delta);
+      continue;
+    }
     if (!fs.use64) {
       assembleFactor<FT, G>(c, st, rootT<FT>(c), ep, ea, fail, wrong, mind);
       if (sizeof(FT) == 4 && (wrong || !isfinite(mind))) {
@@ -1695,13 +1965,7 @@ __device__ __noinline__ bool factorizeWithRetryImpl(Ctx& c, const DevSettings& s
       assembleFactor<typename HighT<FT>::type, G>(c, st, rootHigh<FT>(c), ep, ea, fail, wrong, mind);
     }
     if (threadIdx.x == 0) c.sc[SC_ATTEMPTS] += 1.0;
-    // fault injection (tests): this attempt reports failure
-    const bool injected = c.sc[SC_FAULTF] < (double)st.fault_factor_failures;
     __syncthreads();
-    if (injected) {
-      if (threadIdx.x == 0) c.sc[SC_FAULTF] += 1.0;
-      fail = 1;
-    }
     if (!fail && isfinite(mind) && mind > st.dynamic_reg_eps) {
       fs.ep = ep;
       fs.ea = ea;
@@ -1858,12 +2122,14 @@ __device__ __noinline__ double kktSolveImpl(Ctx& c, const DevSettings& st, FactS
       // escalate: x1000 bumps from the held factor's, up to 10 times
       double ep = fs.ep, ea = fs.ea;
       bool ok = false;
+      const double socEa = ladderBump((int)c.sc[SC_SOCLVL], st.dynamic_reg_delta);
       for (int att = 0; att < 10 && !ok; ++att) {
         ep = fmax(ep * 1000.0, st.dynamic_reg_delta);
         ea = fmax(ea * 1000.0, st.dynamic_reg_delta);
         int fail = 0, wrong = 0;
         double mind = 0.0;
         if (threadIdx.x == 0) c.sc[SC_ESC] += 1.0;
+        if (ea < socEa) continue;  // the reference's SOC-block pivots still fail at this bump
         if (fs.use64)
           assembleFactor<typename HighT<FT>::type, G>(c, st, rootHigh<FT>(c), ep, ea, fail, wrong, mind);
         else
@@ -1974,7 +2240,7 @@ __device__ __noinline__ void solveInstance(Ctx& c, const LaunchArgs& a, int inst
     ensureStrictlyInteriorWarm(c, c.z);
   } else {
     // computeInitialPoint: Hs = I scaling of the identity element, 1 or 2 KKT solves
-    coneUpdateScaling(c, c.ev, c.ev);
+    coneUpdateScaling(c, st, c.ev, c.ev);
     if (!factorizeWithRetry<FT, G>(c, st, fs)) {
       initOk = false;
     } else {
@@ -2027,7 +2293,7 @@ __device__ __noinline__ void solveInstance(Ctx& c, const LaunchArgs& a, int inst
     const double att0 = c.sc[SC_ATTEMPTS];
     __syncthreads();
     // 1. refactorise for the current scaling
-    coneUpdateScaling(c, c.s, c.z);
+    coneUpdateScaling(c, st, c.s, c.z);
     if (!factorizeWithRetry<FT, G>(c, st, fs)) { status = 5; break; }
     if (trow && threadIdx.x == 0) trow[11] = c.sc[SC_ATTEMPTS] - att0;
     // 2. constant solve (-q, b) -> x1, z1; Px1
@@ -2493,10 +2759,22 @@ static __device__ __noinline__ void adjointInstance(Ctx& c, const LaunchArgs& a)
 // Host launchers of the kernels above, per root arithmetic FT (float: mixed precision, double:
 // FP64) and launch form; explicitly instantiated in cxg_ipm_f32.cu, cxg_ipm_f32s.cu,
 // cxg_ipm_f64.cu (batched forms) and cxg_ipm_gridf.cu, cxg_ipm_gridd.cu (whole-GPU form).
+// Raises (never lowers) a kernel's dynamic shared-memory cap. The cap is one attribute of the
+// function, while the size-bucket launches of one kernel form ask for different sizes: setting
+// it to each launch's own size left the cap at the last bucket's, below what the earlier nodes of
+// a captured graph carry, and a profiler replaying one of those nodes then failed to launch it.
+static inline cudaError_t raiseDynSmem(const void* k, size_t smem) {
+  cudaFuncAttributes fa;
+  cudaError_t e = cudaFuncGetAttributes(&fa, k);
+  if (e != cudaSuccess) return e;
+  if ((int)smem <= fa.maxDynamicSharedSizeBytes) return cudaSuccess;
+  return cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+}
+
 template <typename FT, int kMaxThreads, int kMinBlocks>
 cudaError_t launchIpmFormT(const LaunchArgs& a, int grid, int block, size_t smem, cudaStream_t stream) {
   void (*k)(LaunchArgs) = ipmKernel<FT, kMaxThreads, kMinBlocks>;
-  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaError_t e = raiseDynSmem((const void*)k, smem);
   if (e != cudaSuccess) return e;
   k<<<grid, block, smem, stream>>>(a);
   return cudaGetLastError();
@@ -2505,7 +2783,7 @@ cudaError_t launchIpmFormT(const LaunchArgs& a, int grid, int block, size_t smem
 template <typename FT, int kMaxThreads, int kMinBlocks>
 cudaError_t ipmOccupancyFormT(int* blocksPerSM, int block, size_t smem) {
   void (*k)(LaunchArgs) = ipmKernel<FT, kMaxThreads, kMinBlocks>;
-  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaError_t e = raiseDynSmem((const void*)k, smem);
   if (e != cudaSuccess) return e;
   return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocksPerSM, k, block, smem);
 }
@@ -2513,7 +2791,7 @@ cudaError_t ipmOccupancyFormT(int* blocksPerSM, int block, size_t smem) {
 template <typename FT>
 cudaError_t launchIpmGridT(const LaunchArgs& a, GridCtl* g, int grid, size_t smem, cudaStream_t stream) {
   void (*k)(LaunchArgs) = ipmGridKernel<FT>;
-  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaError_t e = raiseDynSmem((const void*)k, smem);
   if (e != cudaSuccess) return e;
   LaunchArgs av = a;
   av.grid = g;
@@ -2524,7 +2802,7 @@ cudaError_t launchIpmGridT(const LaunchArgs& a, GridCtl* g, int grid, size_t sme
 template <typename FT>
 cudaError_t ipmGridOccupancyT(int* blocksPerSM, size_t smem) {
   void (*k)(LaunchArgs) = ipmGridKernel<FT>;
-  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaError_t e = raiseDynSmem((const void*)k, smem);
   if (e != cudaSuccess) return e;
   return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocksPerSM, k, 256, smem);
 }

@@ -63,7 +63,7 @@ __global__ void __launch_bounds__(256) adjointKernel(LaunchArgs a) {
 }
 
 cudaError_t launchAdjoint(const LaunchArgs& a, int grid, int block, size_t smem, cudaStream_t stream) {
-  cudaError_t e = cudaFuncSetAttribute(adjointKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaError_t e = raiseDynSmem((const void*)adjointKernel, smem);
   if (e != cudaSuccess) return e;
   adjointKernel<<<grid, block, smem, stream>>>(a);
   return cudaGetLastError();

@@ -127,7 +127,8 @@ static cudaError_t probeGridLaunch(int nr, int nx, const double* K, const double
   int dev = 0, numSM = 0, occ = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&numSM, cudaDevAttrMultiProcessorCount, dev);
-  const size_t smem = (size_t)gridStageBytes((int)sizeof(T));
+  // FP32: the tensor-core trailing update stages TF32 hi/lo panels (kTcStageBytes)
+  const size_t smem = (size_t)std::max<int64_t>(gridStageBytes((int)sizeof(T)), sizeof(T) == 4 ? kTcStageBytes : 0);
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(denseProbeGridKernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, denseProbeGridKernel<T>, 256, smem);

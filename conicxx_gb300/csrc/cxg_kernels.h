@@ -19,6 +19,11 @@ struct SmemLayout {
   int64_t redOff, vecOff, rootOff, total;
 };
 
+// Shared memory of the whole-GPU FP32 trailing update on the tensor cores: four 16 KB TF32 operand
+// panels (A hi/lo, B hi/lo) and two buffers of the 16 C tiles of a 128x128 super-block, plus
+// 128 bytes of alignment slack.
+constexpr int64_t kGridTcStageBytes = 4 * 16384 + 2 * 16 * (int64_t)kTileElems * 4 + 128;
+
 // Doubles of FP64 vectors per CTA for given maxima (must match the carve-up in ipmKernel).
 inline int64_t vecDoubles(int nMax, int mMax, int nrMax, int nsocMax) {
   auto r2 = [](int64_t v) { return (v + 1) & ~int64_t(1); };

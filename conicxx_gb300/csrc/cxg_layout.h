@@ -119,6 +119,7 @@ struct DevSettings {
   int max_iter, refine_max_iter, mixed_refine_max_iter, linear_solver;
   int equilibrate, warm_start, precision, record_timings;
   int fault_factor_failures, fault_nonfinite_solves;  // test-only fault injection (0 = off)
+  int soc_ref_dense, pad0;  // SOC pivot test and Hs products in the reference's dense form
 };
 
 // Per-instance result written by the kernel (mirrors cxg_info plus internal counters).

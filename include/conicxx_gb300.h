@@ -108,6 +108,18 @@ typedef struct cxg_settings {
                                  (src/conicxx/kkt/kkt_system.cpp:242-264) */
   int fault_nonfinite_solves; /* the first k solves with the factor return a non-finite vector, so
                                  escalateAndResolve's x1000 bumps run (kkt_system.cpp:266-294) */
+  /* ---- GB300 addition ---- */
+  int soc_reference_dense;    /* 1 (default): second-order blocks of up to 8 rows enter two decisions
+                                 in the reference's dense FP64 form Hs = W W
+                                 (second_order_cone.cpp:132-158): a factorisation attempt fails where
+                                 the reference's dense block -(Hs + eps I) has a pivot at or below
+                                 dynamic_reg_eps, as its sparse LDL' of K does near the cone boundary
+                                 (kkt_system.cpp:242-264), and the step directions ds = -(Hs dz + ...)
+                                 use the dense product (cone_set.cpp:70-75). The device's eigen-form
+                                 scaling is otherwise exact to rounding there; the reference's
+                                 convergence on problems with many near-boundary blocks relies on
+                                 the dense form's rounding. 0: eigen-form throughout. The pivot test
+                                 is off with CXG_LINSOLVER_REGULARIZED */
 } cxg_settings;
 
 /* conicxx::Info (include/conicxx/solution.h:18-26) plus Solution::objective/status and counters. */

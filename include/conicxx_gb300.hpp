@@ -180,6 +180,7 @@ struct Settings {
   int threads_per_instance = 0;
   bool differentiable = true;  // keep the final factorisation for backward()
   int whole_gpu_root = 0;      // 0 automatic (roots above 512 rows use every SM), 1 always, -1 never
+  bool soc_reference_dense = true;  // SOC pivot test and Hs products in the reference's dense form
 };
 
 // Status / Info / Solution (include/conicxx/solution.h:9-39).
@@ -287,6 +288,7 @@ inline cxg_settings toC(const Settings& s) {
   c.whole_gpu_root = s.whole_gpu_root;
   c.fault_factor_failures = 0;
   c.fault_nonfinite_solves = 0;
+  c.soc_reference_dense = s.soc_reference_dense ? 1 : 0;
   return c;
 }
 }  // namespace detail

@@ -5,8 +5,13 @@ reference_kats.json  -- the known-answer tests of the reference's own test suite
                         results with their file:line sources.
 oracle_instances.npz -- seeded synthetic instances (contact, random conic QP) with the CPU
                         oracle's solutions (status, iterations, x, s, z, objective).
+oracle_large.npz     -- configuration 2's family (generators.large_sparse_qp, seed 0) at n = 2000
+                        and 3000: the oracle's solutions at the default tolerances (1e-8) and, at
+                        n = 2000, at 1e-10 ("n2000t"), with a checksum of the generated problem
+                        (the problem itself is regenerated from its seed by the tests).
 
-Run from the repository root:  python tests/golden/make_golden.py
+Run from the repository root:  python tests/golden/make_golden.py [--large]
+(--large writes oracle_large.npz only; its oracle solves take several minutes.)
 """
 import json
 import os
@@ -68,6 +73,32 @@ def instances():
     return out
 
 
+def large_family(n):
+    """Configuration 2's family scaled to n variables (the proportions of n = 20000)."""
+    f = n / 20000
+    return generators.large_sparse_qp(0, n=n, m_zero=int(2000 * f), m_nonneg=int(24000 * f), n_soc=int(2000 * f))
+
+
+def problem_checksum(qp):
+    return np.array([qp.P.data.sum(), qp.A.data.sum(), qp.q.sum(), qp.b.sum(), qp.P.nnz, qp.A.nnz])
+
+
+def main_large():
+    import oracle as orc
+
+    orc.build()
+    arrays = {}
+    for n, tol in ((2000, 1e-8), (3000, 1e-8), (2000, 1e-10)):
+        qp = large_family(n)
+        x, s, z, info, _ = orc.solve(qp, warm_start=0, tol_feas=tol, tol_gap_abs=tol, tol_gap_rel=tol)
+        p = f"n{n}/" if tol == 1e-8 else f"n{n}t/"
+        arrays[p + "checksum"] = problem_checksum(qp)
+        arrays[p + "x"], arrays[p + "s"], arrays[p + "z"] = x, s, z
+        arrays[p + "info"] = np.array([info["status"], info["iterations"], info["objective"]])
+        print("large family n", n, "tol", tol, "status", info["status"], "iterations", info["iterations"], flush=True)
+    np.savez_compressed(os.path.join(HERE, "oracle_large.npz"), **arrays)
+
+
 def main():
     import oracle as orc
 
@@ -92,4 +123,7 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    if "--large" in sys.argv:
+        main_large()
+    else:
+        main()

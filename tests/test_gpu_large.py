@@ -2,7 +2,8 @@
 solved by every SM (cooperative launch), CTA 0 running the interior-point iteration.
 
 - The factor itself (cxg_dense_ldlt, threads = -1) gives the same L and D bits as the one-CTA
-  root: every tile receives the same updates in the same order.
+  root in FP64 and double-float (every tile receives the same updates in the same order); in FP32
+  the trailing update runs on the tensor cores (3xTF32), and L and D agree to FP32 accuracy.
 - Full solves (whole_gpu_root = 1) against the oracle: same status, iterations within +-1,
   x within 1e-6 relative; and against the one-CTA form of the same instance.
 - The large single-instance workloads at full size (n = 20000, m = 30000 sparse QP): status and
@@ -58,15 +59,22 @@ def _probe(K, nx, b, arith, threads):
 @pytest.mark.parametrize("arith", ["fp64", "fp32", "df64"])
 @pytest.mark.parametrize("nr,nx", [(40, 30), (150, 120), (190, 160)])
 def test_grid_factor_equals_one_cta(arith, nr, nx):
-    """The whole-GPU LDL' is bit-identical to the one-CTA LDL' (same tile operations in the same
-    order per tile); its solve agrees with numpy to the arithmetic's accuracy. Sizes up to six
-    tiles, the largest 8-byte root the one-CTA probe holds in shared memory."""
+    """The whole-GPU LDL' is bit-identical to the one-CTA LDL' in FP64 and double-float (same tile
+    operations in the same order per tile); in FP32 its trailing updates run on the tensor cores
+    as 3xTF32 products, so L and D agree to FP32 accuracy. Its solve agrees with numpy to the
+    arithmetic's accuracy. Sizes up to six tiles, the largest 8-byte root the one-CTA probe holds
+    in shared memory."""
     K = _quasi_definite(nr, nx, nr + 7)
     b = np.random.default_rng(nr).standard_normal(nr)
     L1, D1, x1, f1 = _probe(K, nx, b, arith, 256)
     Lg, Dg, xg, fg = _probe(K, nx, b, arith, -1)
     assert fg[2] == 0 and fg[0] == 0 and fg[1] == 0 and f1[0] == 0 and f1[1] == 0
-    assert np.array_equal(L1, Lg) and np.array_equal(D1, Dg)
+    if arith == "fp32":
+        # FP32-level agreement (a single TF32 product would differ by ~1e-3)
+        assert np.max(np.abs(L1 - Lg)) < 1e-5 * max(1.0, np.max(np.abs(L1)))
+        assert np.max(np.abs(D1 - Dg) / np.abs(D1)) < 1e-5
+    else:
+        assert np.array_equal(L1, Lg) and np.array_equal(D1, Dg)
     xs = np.linalg.solve(K, b)
     tol = {"fp64": 1e-10, "df64": 1e-8, "fp32": 1e-3}[arith]
     assert rel(xg, xs) < tol and rel(x1, xs) < tol
@@ -83,7 +91,9 @@ def test_grid_factor_large_root(arith):
     xs = np.linalg.solve(K, b)
     tol = {"fp64": 1e-10, "df64": 1e-8, "fp32": 1e-3}[arith]
     assert rel(x, xs) < tol
-    assert rel(L @ np.diag(D) @ L.T, K) < tol
+    # FP32 (tensor-core 3xTF32 trailing updates): the reconstruction at FP32 accuracy, well below
+    # the ~1e-3 of a single TF32 product
+    assert rel(L @ np.diag(D) @ L.T, K) < (1e-5 if arith == "fp32" else tol)
 
 
 @pytest.mark.parametrize("precision", [_abi.PRECISION_FP64, _abi.PRECISION_MIXED])
@@ -191,22 +201,81 @@ def test_whole_gpu_warm_start_and_backward(oracle_mod):
 
 
 def test_large_sparse_qp_full_size_mixed():
-    """The n = 20000, m = 30000 sparse QP (root of 22000 rows) in mixed precision on the whole GPU:
-    a definite status; when Solved, the returned point meets the tolerances on the unscaled KKT
-    conditions (a property independent of the oracle, which does not finish at this size)."""
+    """Configuration 2 at full size: the n = 20000, m = 30000 sparse QP (root of 22000 rows) in
+    mixed precision on the whole GPU is Solved, and the returned point meets the tolerances on the
+    unscaled KKT conditions (a property independent of the oracle, which takes hours at this
+    size; its parity cases are the same family at n = 2000 and 3000, below)."""
     from conicxx_gb300 import Solver
 
     qp = generators.large_sparse_qp(0)
     S = Solver()
-    # 20 iterations (about 1.3 s each once the factor is double-float); the full run ends at
-    # MaxIterations after 200, as the oracle does on this family at n = 2000
-    assert S.setup(qp, precision=_abi.PRECISION_MIXED, warm_start=0, max_iter=20)
+    assert S.setup(qp, precision=_abi.PRECISION_MIXED, warm_start=0)
     sol = S.solve()
-    assert sol.status in (_abi.STATUS_SOLVED, _abi.STATUS_MAX_ITERATIONS)
-    assert np.all(np.isfinite(sol.x))
-    if sol.status == _abi.STATUS_SOLVED:
-        st, fe, sz = qp.kkt_residuals(sol.x, sol.s, sol.z)
-        assert fe < 1e-5 and sz < 1e-5
+    assert sol.status == _abi.STATUS_SOLVED, (sol.status_name, sol.info["iterations"])
+    assert sol.info["iterations"] <= 40
+    st, fe, sz = qp.kkt_residuals(sol.x, sol.s, sol.z)
+    scale = max(1.0, np.linalg.norm(qp.q), np.linalg.norm(qp.b))
+    assert st < 1e-6 * scale and fe < 1e-6 * scale and abs(sz) < 1e-6 * max(1.0, abs(sol.objective)), (st, fe, sz)
+    assert np.all(qp.cone_margins(sol.s)[0] >= -1e-9) and np.all(qp.cone_margins(sol.z)[0] >= -1e-9)
+
+
+def _golden_large():
+    import os
+
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "oracle_large.npz")
+    return np.load(path)
+
+
+@pytest.mark.parametrize("precision", [_abi.PRECISION_FP64, _abi.PRECISION_MIXED])
+@pytest.mark.parametrize("n", [2000, 3000])
+def test_large_family_agrees_with_oracle_golden(n, precision):
+    """Configuration 2's family at n = 2000 and 3000 (roots of 2200 and 3300 rows) on the whole
+    GPU against the oracle's solutions (tests/golden/oracle_large.npz): both Solved; x, s and z
+    within 5e-5 relative to their max-norm, the size of the 1e-8 stopping ball on this family
+    (P = M'M + 1e-3 I): the oracle's own solutions at 1e-8 and at 1e-10 differ by 1.6e-5 (x),
+    4.6e-5 (s) and 3.3e-5 (z) at n = 2000 (its 1e-10 solution is kept in the fixture as n2000t).
+    Iteration counts are not compared: past the point where the reference's dense SOC blocks
+    lose their small eigenvalue, its path depends on their rounding (the device holds those
+    blocks at the dense form's resolution instead; 12-13 iterations against the oracle's 20-26)."""
+    from conicxx_gb300 import Solver
+
+    g = _golden_large()
+    f = n / 20000  # the proportions of n = 20000 (tests/golden/make_golden.py, large_family)
+    qp = generators.large_sparse_qp(0, n=n, m_zero=int(2000 * f), m_nonneg=int(24000 * f), n_soc=int(2000 * f))
+    checksum = [qp.P.data.sum(), qp.A.data.sum(), qp.q.sum(), qp.b.sum(), qp.P.nnz, qp.A.nnz]
+    np.testing.assert_allclose(checksum, g[f"n{n}/checksum"], rtol=1e-12)
+    S = Solver()
+    assert S.setup(qp, precision=precision, warm_start=0, whole_gpu_root=1)
+    sol = S.solve()
+    status_o = int(g[f"n{n}/info"][0])
+    assert sol.status == status_o == _abi.STATUS_SOLVED, (sol.status_name, sol.info["iterations"])
+    for name, v in (("x", sol.x), ("s", sol.s), ("z", sol.z)):
+        vo = g[f"n{n}/{name}"]
+        err = np.max(np.abs(v - vo)) / max(1.0, np.max(np.abs(vo)))
+        print("n=%d %s error vs oracle %.2e" % (n, name, err))
+        assert err < 5e-5, (name, err)
+
+
+def test_large_family_mixed_equals_fp64_factor():
+    """FP32 factorisation with FP64 refinement against the FP64 factorisation on the same
+    instance of configuration 2's family (n = 4000): both Solved, x, s and z within 1e-6
+    (measured 3e-12, 3e-10, 5e-12: the two runs take the same path)."""
+    from conicxx_gb300 import Solver
+
+    f = 4000 / 20000
+    qp = generators.large_sparse_qp(0, n=4000, m_zero=int(2000 * f), m_nonneg=int(24000 * f), n_soc=int(2000 * f))
+    sols = []
+    for precision in (_abi.PRECISION_MIXED, _abi.PRECISION_FP64):
+        S = Solver()
+        assert S.setup(qp, precision=precision, warm_start=0)
+        sol = S.solve()
+        assert sol.status == _abi.STATUS_SOLVED, (precision, sol.status_name)
+        sols.append(sol)
+    for name in ("x", "s", "z"):
+        a, b = getattr(sols[0], name), getattr(sols[1], name)
+        err = np.max(np.abs(a - b)) / max(1.0, np.max(np.abs(b)))
+        print("mixed vs FP64 factor, %s: %.2e" % (name, err))
+        assert err < 1e-6, name
 
 
 def test_grid_barrier_wait_runs_out_and_reports():

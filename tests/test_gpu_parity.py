@@ -15,6 +15,7 @@ import pytest
 from conftest import kat_qp, rel
 from conicxx_gb300 import _abi, _lib, generators
 from conicxx_gb300._abi import dptr, iptr
+from conicxx_gb300.problem import sym_upper_matvec
 
 pytestmark = pytest.mark.gpu
 
@@ -238,8 +239,7 @@ def test_golden_instances(golden_instances, precision):
         assert S.setup(qp, precision=precision)
         sol = S.solve()
         assert sol.status == exp["status"], (name, sol.status_name)
-        assert abs(sol.info["iterations"] - exp["iterations"]) <= 1 or sol.info["iterations"] < exp["iterations"], \
-            (name, sol.info["iterations"], exp["iterations"])
+        assert abs(sol.info["iterations"] - exp["iterations"]) <= 1, (name, sol.info["iterations"], exp["iterations"])
         for a, b, tol in ((sol.x, exp["x"], X_TOL), (sol.s, exp["s"], SZ_TOL), (sol.z, exp["z"], SZ_TOL)):
             assert rel(a, b) < tol, (name, rel(a, b))
         assert sol.info["primal_residual"] < 1e-8 and sol.info["dual_residual"] < 1e-8
@@ -295,34 +295,59 @@ def test_full_size_contact_batch_properties():
 @pytest.mark.parametrize("precision", [_abi.PRECISION_MIXED, _abi.PRECISION_FP64])
 def test_full_size_contact_batch_agrees_with_oracle(oracle_mod, precision):
     """The 4096-instance contact batch against the oracle solving the same instances on the host
-    (one thread per instance): the same status on >= 99.5% of instances (the rest are
-    borderline instances whose last iterate sits on the 1e-8 threshold, where either solver's
-    rounding decides Solved vs MaxIterations); iterations within +-1 on >= 95% of the instances
-    both solve; x within 1e-6 relative (max-norm scaled) on >= 90% of a sample of them and within
-    1e-4 on all. The tail (measured: median 2e-10, p90 2e-7, p99 4e-6) is instances whose
-    stopping iterate differs by an iteration: P = J Minv J' + 1e-6 I is rank deficient up to the
-    1e-6 shift, so x is determined only to about tol / 1e-6 at the 1e-8 stopping point."""
+    (one thread per instance), compared on every instance:
+    - the same status on >= 99.5% of instances; the rest are listed: borderline instances whose
+      last iterate sits on the 1e-8 threshold, where either solver's rounding decides Solved vs
+      MaxIterations;
+    - on every instance both solve: iterations within +-1 on >= 95%;
+    - x and s within 1e-6 relative (max-norm scaled) on >= 95% and within 1e-4 on all (measured:
+      median 7e-10, 95.5% within 1e-6, max 3e-5). The tail is instances whose stopping iterate
+      differs by an iteration: P = J Minv J' + 1e-6 I is rank deficient up to the 1e-6 shift, so
+      x is determined only to about tol / 1e-6 at the 1e-8 stopping point;
+    - z: wherever it differs from the oracle's by more than 1e-6, the device's (x, s, z) meets the
+      KKT conditions of the original problem to 1e-6 (stationarity, feasibility, s'z), i.e. it
+      is another optimal dual: the duals are not unique on contacts whose normal force vanishes,
+      where the normal row and the friction cone's apex are both active."""
     _, BatchSolver = _solvers()
     qps = generators.contact_batch(4096)
     B = BatchSolver(qps, warm_start=0, precision=precision)
     x, s, z, infos = B.solve()
     st, it = infos["status"], infos["iterations"]
-    _, ost, oit = oracle_mod.batch_solve(qps, os.cpu_count() or 1, warm_start=0)
+    _, ost, oit, ox, os_, oz = oracle_mod.batch_solve_x(qps, os.cpu_count() or 1, warm_start=0)
     agree = st == ost
+    print("status agreement %d/%d, mismatches (index, gpu, oracle):" % (agree.sum(), len(qps)),
+          [(int(i), int(st[i]), int(ost[i])) for i in np.where(~agree)[0]])
     assert agree.mean() >= 0.995, (agree.sum(), np.where(~agree)[0][:20])
     both = agree & (st == 1)
     d = it[both] - oit[both]
     assert np.mean(np.abs(d) <= 1) >= 0.95, dict(zip(*np.unique(d, return_counts=True)))
-    # x against the oracle's x on a sample of commonly solved instances
-    idx = np.where(both)[0][::16]
-    errs = []
-    xs = B.split(x, s, z)
-    for i in idx:
-        xo = oracle_mod.solve(qps[i], warm_start=0)[0]
-        errs.append(np.max(np.abs(xs[i][0] - xo)) / max(1.0, np.max(np.abs(xo))))
-    errs = np.array(errs)
-    print("x error vs oracle: median %.2e p90 %.2e p99 %.2e max %.2e" % (*np.percentile(errs, [50, 90, 99]), errs.max()))
-    assert np.mean(errs < 1e-6) >= 0.9 and errs.max() < 1e-4, np.percentile(errs, [50, 90, 99])
+    gs, os2 = B.split(x, s, z), B.split(ox, os_, oz)
+    errs = {"x": [], "s": [], "z": []}
+    bad_dual = []
+    for i in np.where(both)[0]:
+        for k, key in enumerate(("x", "s", "z")):
+            g, o = gs[i][k], os2[i][k]
+            errs[key].append(np.max(np.abs(g - o)) / max(1.0, np.max(np.abs(o))))
+        if errs["z"][-1] > 1e-6:
+            # the device's point is a KKT point as good as the oracle's own: stationarity and
+            # feasibility within 1e-6 of the data's scale, s'z within the oracle's own s'z (or
+            # the 1e-8 gap tolerance of the objective)
+            g_res = qps[i].kkt_residuals(*gs[i])
+            o_res = qps[i].kkt_residuals(*os2[i])
+            scale = max(1.0, np.linalg.norm(qps[i].q), np.linalg.norm(qps[i].b))
+            obj = abs(float(0.5 * gs[i][0] @ sym_upper_matvec(qps[i].P, gs[i][0]) + qps[i].q @ gs[i][0]))
+            ok = (g_res[0] < 1e-6 * scale and g_res[1] < 1e-6 * scale
+                  and abs(g_res[2]) <= max(10.0 * abs(o_res[2]), 1e-8 * max(1.0, obj)))
+            if not ok:
+                bad_dual.append((int(i), g_res, o_res))
+    errs = {k: np.array(v) for k, v in errs.items()}
+    for k, v in errs.items():
+        print("%s error vs oracle over %d instances: median %.2e p99 %.2e max %.2e, <= 1e-6: %.4f"
+              % (k, v.size, np.median(v), np.percentile(v, 99), v.max(), np.mean(v <= 1e-6)))
+    for k in ("x", "s"):
+        assert np.mean(errs[k] <= 1e-6) >= 0.95 and errs[k].max() < 1e-4, k
+    print("z beyond 1e-6 of the oracle's on %d instances, each a KKT point of its problem" % np.sum(errs["z"] > 1e-6))
+    assert not bad_dual, bad_dual[:10]
 
 
 @pytest.mark.parametrize("precision", [_abi.PRECISION_MIXED, _abi.PRECISION_FP64])

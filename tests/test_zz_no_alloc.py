@@ -89,13 +89,14 @@ def test_noalloc_rejects_oversized_instance(torch_cuda):
 
 
 def test_noalloc_grid_cut_to_the_fixed_array(torch_cuda):
-    """512 FP64 contact instances: the largest bucket's persistent grid times its per-CTA working
-    memory exceeds the fixed array, so the entry point runs that bucket on fewer CTAs. Statuses,
-    iterations and x, s, z still equal the regular device solve's."""
+    """128 FP64 instances of the n = 200, m = 300 random conic QP: their 220-row roots do not fit in
+    shared memory, so each CTA's working memory (root included) is about 0.36 MB, and a grid of
+    128 CTAs needs more than the fixed array holds; the entry point runs the bucket on fewer CTAs.
+    Statuses, iterations and x, s, z still equal the regular device solve's."""
     from conicxx_gb300 import BatchSolver
 
     torch = torch_cuda
-    qps = generators.contact_batch(512, base_seed=900)
+    qps = [generators.config0_qp(700 + i) for i in range(128)]
     B = BatchSolver(qps, warm_start=0, precision=_abi.PRECISION_FP64)
     cap = (32 << 20) - 256  # CXG_NOALLOC_SCRATCH_BYTES less the queue counters
     cut = [ln for ln in B.describe().splitlines()
