@@ -317,7 +317,7 @@ def run_gb300(args, rank, world, local_rank):
                   "cpu_1core_ms": float(np.median(c_ms)), "iterations_gpu_mixed": int(sol0m.info["iterations"]),
                   "iterations_gpu": int(sol0.info["iterations"]), "iterations_cpu": int(oi0["iterations"]),
                   "status_gpu": int(sol0.status), "status_cpu": int(oi0["status"])}
-        large = large_instance_leg(orc)
+        large = large_instance_leg(orc, args.large_fp64, args.large_full)
         # ---- the same batch with the FP64 factor (configuration 1 names FP64 and mixed) ----
         B64 = BatchSolver(qps, settings=default_settings(precision=0, warm_start=0))
         dx64 = torch.empty_like(dx)
@@ -443,13 +443,15 @@ def parity_summary(sample, B, infos, cpu_st, cpu_it, gpu, orc_):
     return out
 
 
-def large_instance_leg(orc):
+def large_instance_leg(orc, fp64_factor=False, groups_full=False):
     """Single large instances on the whole GPU (root spread over every SM), mixed precision:
     - the n=20000, m=30000 sparse QP (root of 22000 rows): the full solve to 1e-8 (status,
       iterations, time, KKT residuals of the returned point), and its first 3 iterations alone
       for the FP32 factor's throughput (tensor-core trailing updates);
+    - with fp64_factor, the same instance solved again with the FP64 factor (precision 0), and
+      the largest differences of x, s and z between the two runs;
     - the group-lasso SOCP with 1000 groups of 16 (n=17000, 1000 SOC blocks of dimension 17),
-      solved to completion;
+      solved to completion; with groups_full, also at 4000 groups (n=68000, a 68000-row root);
     - the sparse QP family at n=1000 (root of 1100 rows) against the oracle on one host core."""
     from conicxx_gb300 import Solver, generators
 
@@ -494,19 +496,41 @@ def large_instance_leg(orc):
         "factor_attempts": int(inf["factor_attempts"]), "ldlt_s": inf["time_ldlt_s"],
         "dense_solve_s": inf["time_dense_solve_s"], "max_relres": inf["max_relres"],
         "kkt_residuals": [float(st_), float(fe_), float(sz_)], "first_3_iterations": first3}
-    qpg = generators.group_lasso_socp(0, groups=1000)
-    S = Solver()
-    assert S.setup(qpg, precision=1, warm_start=0, record_timings=1)
-    t0 = time.perf_counter()
-    sol = S.solve()
-    dt = time.perf_counter() - t0
-    inf = sol.info
-    st_, fe_, sz_ = qpg.kkt_residuals(sol.x, sol.s, sol.z)
-    out["group_lasso_g1000"] = {
-        "workload": "1000 groups of 16: n=17000, F 20000 x 16000 (12 nnz/row, 64 blocks + 5% coupling), 1000 Q^17",
-        "solve_s": dt, "status": int(sol.status), "iterations": int(inf["iterations"]),
-        "fp64_fallbacks": int(inf["fp64_fallbacks"]), "ldlt_s": inf["time_ldlt_s"],
-        "dense_solve_s": inf["time_dense_solve_s"], "kkt_residuals": [float(st_), float(fe_), float(sz_)]}
+    if fp64_factor:
+        S64 = Solver()
+        assert S64.setup(qp, precision=0, warm_start=0, record_timings=1)
+        t0 = time.perf_counter()
+        sol64 = S64.solve()
+        dt64 = time.perf_counter() - t0
+        inf64 = sol64.info
+        r64 = qp.kkt_residuals(sol64.x, sol64.s, sol64.z)
+
+        def rdiff(a, b):
+            return float(np.max(np.abs(a - b)) / max(1.0, float(np.max(np.abs(b)))))
+
+        out["sparse_qp_n20000"]["fp64_factor"] = {
+            "status": int(sol64.status), "iterations": int(inf64["iterations"]), "solve_s": dt64,
+            "factor_attempts": int(inf64["factor_attempts"]), "ldlt_s": inf64["time_ldlt_s"],
+            "kkt_residuals": [float(v) for v in r64],
+            "objective_mixed": float(sol.objective), "objective_fp64": float(sol64.objective),
+            "mixed_vs_fp64": {"x": rdiff(sol.x, sol64.x), "s": rdiff(sol.s, sol64.s), "z": rdiff(sol.z, sol64.z),
+                              "metric": "max |v_mixed - v_fp64| / max(1, max |v_fp64|)"}}
+    for groups in ((1000, 4000) if groups_full else (1000,)):
+        qpg = generators.group_lasso_socp(0, groups=groups)
+        S = Solver()
+        assert S.setup(qpg, precision=1, warm_start=0, record_timings=1)
+        t0 = time.perf_counter()
+        sol = S.solve()
+        dt = time.perf_counter() - t0
+        inf = sol.info
+        st_, fe_, sz_ = qpg.kkt_residuals(sol.x, sol.s, sol.z)
+        out["group_lasso_g%d" % groups] = {
+            "workload": "%d groups of 16: n=%d, F %d x %d (12 nnz/row, 64 blocks + 5%% coupling), %d Q^17"
+                        % (groups, 17 * groups, 20 * groups, 16 * groups, groups),
+            "root_rows": qpg.n + qpg.zero, "solve_s": dt, "status": int(sol.status),
+            "iterations": int(inf["iterations"]), "fp64_fallbacks": int(inf["fp64_fallbacks"]),
+            "factor_attempts": int(inf["factor_attempts"]), "ldlt_s": inf["time_ldlt_s"],
+            "dense_solve_s": inf["time_dense_solve_s"], "kkt_residuals": [float(st_), float(fe_), float(sz_)]}
     qps = generators.large_sparse_qp(0, n=1000, m_zero=100, m_nonneg=1200, n_soc=100)
     times = {}
     for prec in (0, 1):
@@ -617,8 +641,13 @@ def main():
     ap.add_argument("--entry", default="graph", choices=["graph", "noalloc"],
                     help="graph: the captured concurrent-bucket solve (default); noalloc: the allocation-free "
                          "entry point (direct launches, buckets in sequence)")
-    ap.add_argument("--legs", default="all", choices=["all", "main"],
-                    help="main: only the device-resident batched timing (profiling runs)")
+    ap.add_argument("--legs", default="all", choices=["all", "main", "large"],
+                    help="main: only the device-resident batched timing (profiling runs); large: only the "
+                         "single large instances (configurations 2 and 4) on the whole GPU")
+    ap.add_argument("--large-fp64", action="store_true",
+                    help="large instances: also solve configuration 2 with the FP64 factor and compare")
+    ap.add_argument("--large-full", action="store_true",
+                    help="large instances: also solve configuration 4 at full size (4000 groups)")
     ap.add_argument("--probe-ldlt", type=int, default=0, metavar="NR",
                     help="instead of the benchmark: time the dense root LDL' alone on an NR-row matrix")
     ap.add_argument("--probe-arith", default="fp32", choices=["fp64", "fp32", "df64"])
@@ -636,6 +665,17 @@ def main():
         for _ in range(args.probe_repeat):
             print(json.dumps(ldlt_probe(nr, max(1, nr - 256), args.probe_arith, args.probe_threads,
                                         check=args.probe_check)), flush=True)
+        return
+    if args.legs == "large":
+        if not os.path.exists(os.path.join(ROOT, "conicxx_gb300", "_build", "libconicxx_gb300.so")):
+            import __graft_entry__
+
+            __graft_entry__.build()
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle as orc
+
+        orc.build()
+        print(json.dumps({"large_instance": large_instance_leg(orc, args.large_fp64, args.large_full)}), flush=True)
         return
     if args.impl == "reference":
         out = run_reference(args, rank, world)

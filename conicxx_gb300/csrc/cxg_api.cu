@@ -115,6 +115,8 @@ struct Group {
   int64_t stride = 0;        // scratch doubles per CTA
   int64_t scratchOff = 0;    // offset of this group's scratch in the batch scratch buffer
   int occupancy = 1;         // resident CTAs per SM of this bucket's launch shape
+  int gridAlone = 1;         // persistent grid when the bucket runs alone (occupancy x SMs, capped by count)
+  double work = 0.0;         // estimated SM time per iteration: sum over its instances of nr
   int counterIdx = 0;
 };
 
@@ -236,6 +238,83 @@ static int chooseBlock(int nrMax, int requested) {
   return 256;
 }
 
+// The size buckets run concurrently, one persistent launch each. A launch takes every SM it can
+// hold as soon as it starts, so with full-GPU grids the buckets launched later only start when
+// earlier ones drain their queues, and their slowest instances then end the batch. Instead the
+// SMs are apportioned among the buckets in proportion to their estimated work, so that every
+// bucket's CTAs are resident from the start and the buckets finish together. Measured on the
+// contact batch, the SM time of an instance's iteration grows about linearly with its root size
+// nr: about 5 us x nr where a CTA has its SM to itself, about 3 us x nr where several CTAs share
+// one (their latency-bound chains overlap). A bucket's work is therefore the sum of its
+// instances' nr, times 0.6 for launch shapes with several CTAs per SM (iteration counts are
+// alike across buckets). A bucket never gets more SMs than its instances can fill; the rest go
+// to the others (largest-remainder apportionment).
+static void partitionGrids(cxg_batch* B, int numSM) {
+  const size_t G = B->groups.size();
+  if (B->gridMode) {  // one cooperative launch over every SM
+    for (Group& g : B->groups) g.gridAlone = g.grid;
+    return;
+  }
+  for (Group& g : B->groups) g.gridAlone = std::max(1, std::min(g.count, g.occupancy * numSM));
+  if (G <= 1 || (int)G > numSM) {
+    for (Group& g : B->groups) g.grid = g.gridAlone;
+    return;
+  }
+  std::vector<int> sms(G, 0), need(G);
+  std::vector<bool> capped(G, false);
+  auto weight = [&](size_t b) {
+    const Group& g = B->groups[b];
+    return std::max(g.work, 1.0) * (g.occupancy > 1 ? 0.6 : 1.0);
+  };
+  for (size_t b = 0; b < G; ++b) {
+    const Group& g = B->groups[b];
+    need[b] = std::max(1, (g.count + g.occupancy - 1) / g.occupancy);
+  }
+  int freeSM = numSM;
+  for (bool again = true; again;) {
+    again = false;
+    double w = 0.0;
+    for (size_t b = 0; b < G; ++b)
+      if (!capped[b]) w += weight(b);
+    for (size_t b = 0; b < G && !again; ++b) {
+      if (capped[b]) continue;
+      const double share = freeSM * weight(b) / w;
+      if (share >= need[b]) {  // more SMs than its instances fill: give it what it can use
+        sms[b] = need[b];
+        capped[b] = true;
+        freeSM -= need[b];
+        again = true;
+      }
+    }
+  }
+  double w = 0.0;
+  int open = 0;
+  for (size_t b = 0; b < G; ++b)
+    if (!capped[b]) {
+      w += weight(b);
+      ++open;
+    }
+  if (open > 0) {
+    std::vector<std::pair<double, size_t>> frac;
+    int used = 0;
+    for (size_t b = 0; b < G; ++b) {
+      if (capped[b]) continue;
+      const double share = std::max(freeSM, open) * weight(b) / w;
+      sms[b] = std::max(1, (int)share);
+      used += sms[b];
+      frac.push_back({share - (double)(int)share, b});
+    }
+    std::sort(frac.begin(), frac.end(), [](const std::pair<double, size_t>& a, const std::pair<double, size_t>& c) {
+      return a.first > c.first;
+    });
+    for (size_t k = 0; used < freeSM && k < frac.size(); ++k, ++used) sms[frac[k].second] += 1;
+  }
+  for (size_t b = 0; b < G; ++b) {
+    Group& g = B->groups[b];
+    g.grid = std::max(1, std::min(g.count, sms[b] * g.occupancy));
+  }
+}
+
 static int buildGroups(cxg_batch* B) {
   const int N = B->count;
   const bool fp32 = B->st.precision == CXG_PRECISION_MIXED;
@@ -282,6 +361,7 @@ static int buildGroups(cxg_batch* B) {
       L.mMax = std::max(L.mMax, D.m);
       L.nrMax = std::max(L.nrMax, D.nr);
       L.nsocMax = std::max(L.nsocMax, D.nsoc);
+      g.work += (double)D.nr;  // scaled by the launch shape's sharing in partitionGrids
     }
     const int64_t redBytes = (128 + 32) * 8;
     const int64_t vecBytes = vecDoubles(L.nMax, L.mMax, L.nrMax, L.nsocMax) * 8;
@@ -348,6 +428,7 @@ static int buildGroups(cxg_batch* B) {
       const cudaError_t oe = ipmOccupancy(&occ, g.block, g.smem, fp32);
       if (oe != cudaSuccess || occ < 1) occ = 1;
       g.grid = std::max(1, std::min(g.count, occ * numSM));
+      g.gridAlone = g.grid;
       g.occupancy = occ;
       g.scratchOff = scratchTotal;
       scratchTotal += g.stride * g.grid;
@@ -356,20 +437,11 @@ static int buildGroups(cxg_batch* B) {
     B->groups.push_back(g);
     s = e;
   }
-  // Buckets whose CTAs need a whole SM (one resident per SM) run first and would otherwise hold
-  // every SM until their queues drain, so the small-root buckets (many CTAs per SM, cheap in bulk)
-  // would start last and their slowest instances would end the batch. Leave a fifth of the SMs
-  // to the small buckets from the start.
-  bool haveSmall = false;
-  for (const Group& g : B->groups) haveSmall |= g.occupancy > 1;
-  if (haveSmall) {
-    const int cap = std::max(1, numSM - numSM / 5);
-    scratchTotal = 0;
-    for (Group& g : B->groups) {
-      if (g.occupancy == 1) g.grid = std::min(g.grid, cap);
-      g.scratchOff = scratchTotal;
-      scratchTotal += g.stride * g.grid;
-    }
+  partitionGrids(B, numSM);
+  scratchTotal = 0;
+  for (Group& g : B->groups) {
+    g.scratchOff = scratchTotal;
+    scratchTotal += g.stride * g.grid;
   }
   // scratch
   if (B->dScratch) cudaFree(B->dScratch);
@@ -734,10 +806,19 @@ static int enqueueSolve(cxg_batch* B, cudaStream_t s) {
   const DevSettings ds = makeDevSettings(B->st, B->kktSt);
   CX_CUDA(cudaMemsetAsync(B->dCounters, 0, sizeof(int) * (B->groups.size() + 1), s));
   const size_t G = B->groups.size();
-  while (B->groupStreams.size() < G) {
-    cudaStream_t gs;
-    CX_CUDA(cudaStreamCreateWithFlags(&gs, cudaStreamNonBlocking));
-    B->groupStreams.push_back(gs);
+  // one stream per launch rank, the first the highest priority: the block scheduler dispatches
+  // pending CTAs by stream priority, so the placement follows the launch order below even where
+  // the graph submits its independent launches in another order
+  if (B->groupStreams.size() < G) {
+    int least = 0, greatest = 0;
+    CX_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+    while (B->groupStreams.size() < G) {
+      const int rank = (int)B->groupStreams.size();
+      const int prio = std::min(least, greatest + rank);
+      cudaStream_t gs;
+      CX_CUDA(cudaStreamCreateWithPriority(&gs, cudaStreamNonBlocking, prio));
+      B->groupStreams.push_back(gs);
+    }
   }
   while (B->forkJoin.size() < G + 1) {
     cudaEvent_t e;
@@ -753,19 +834,18 @@ static int enqueueSolve(cxg_batch* B, cudaStream_t s) {
     return CXG_OK;
   }
   CX_CUDA(cudaEventRecord(B->forkJoin[0], s));
-  // Launch order: the largest-root bucket first (its slowest instances are the longest), then the
-  // buckets with several CTAs per SM (cheap in bulk; they take the SMs the large buckets leave
-  // free), then the remaining whole-SM buckets.
-  std::vector<size_t> launchOrder;
-  launchOrder.reserve(G);
-  if (G > 0) launchOrder.push_back(0);
-  for (size_t gi = 1; gi < G; ++gi)
-    if (B->groups[gi].occupancy > 1) launchOrder.push_back(gi);
-  for (size_t gi = 1; gi < G; ++gi)
-    if (B->groups[gi].occupancy <= 1) launchOrder.push_back(gi);
-  for (size_t gi : launchOrder) {
+  // Launch order: by shared memory per CTA, largest first. The grids are apportioned so that all
+  // of them can be resident at once (partitionGrids); the block scheduler spreads each launch's
+  // CTAs over the SMs with room left, so the largest CTAs must be placed before the small ones
+  // scatter over every SM and leave no SM with room for a large one (first fit, decreasing).
+  std::vector<size_t> launchOrder(G);
+  std::iota(launchOrder.begin(), launchOrder.end(), size_t(0));
+  std::stable_sort(launchOrder.begin(), launchOrder.end(),
+                   [&](size_t a_, size_t b_) { return B->groups[a_].smem > B->groups[b_].smem; });
+  for (size_t rank = 0; rank < G; ++rank) {
+    const size_t gi = launchOrder[rank];
     const Group& g = B->groups[gi];
-    cudaStream_t gs = (G == 1) ? s : B->groupStreams[gi];
+    cudaStream_t gs = (G == 1) ? s : B->groupStreams[rank];
     if (G > 1) CX_CUDA(cudaStreamWaitEvent(gs, B->forkJoin[0], 0));
     const LaunchArgs a = solveArgs(B, g, ds, B->dCounters + g.counterIdx, B->dScratch + g.scratchOff);
     CX_CUDA(launchIpm(a, g.grid, g.block, g.smem, g.fp32, gs));
@@ -797,7 +877,7 @@ static int runSolve(cxg_batch* B, cudaStream_t s) {
     if (rc) { if (g) cudaGraphDestroy(g); return rc; }
     if (ce != cudaSuccess) return setErr(CXG_E_CUDA, std::string("graph capture: ") + cudaGetErrorString(ce));
     B->graph = g;
-    CX_CUDA(cudaGraphInstantiate(&B->graphExec, B->graph, 0));
+    CX_CUDA(cudaGraphInstantiate(&B->graphExec, B->graph, cudaGraphInstantiateFlagUseNodePriority));
     B->graphSettings = ds;
     B->graphValid = true;
   }
@@ -1007,13 +1087,18 @@ extern "C" int cxg_batch_autotune(cxg_batch* B, int trials, char* report, int re
     cudaFree(trialScratch);
     if (rc) break;
     g.block = bestBlock;
-    g.grid = bucketGrid(g, bestBlock, numSM);
+    {
+      int occ = 0;
+      if (ipmOccupancy(&occ, bestBlock, g.smem, g.fp32) != cudaSuccess || occ < 1) occ = 1;
+      g.occupancy = occ;
+    }
     std::snprintf(line, sizeof(line), " -> %d\n", bestBlock);
     rep += line;
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   if (rc) return rc;
+  partitionGrids(B, numSM);
   if ((rc = relayoutScratch(B))) return rc;
   B->graphValid = false;  // the captured launch shapes are stale
   if (report && reportLen > 0) std::snprintf(report, (size_t)reportLen, "%s", rep.c_str());
@@ -1154,19 +1239,18 @@ static int enqueueAdjoint(cxg_batch* B, cudaStream_t s, const double* gx, double
   CX_CUDA(cudaMemsetAsync(B->dCounters, 0, sizeof(int) * (B->groups.size() + 1), s));
   const size_t G = B->groups.size();
   CX_CUDA(cudaEventRecord(B->forkJoin[0], s));
-  // Launch order: the largest-root bucket first (its slowest instances are the longest), then the
-  // buckets with several CTAs per SM (cheap in bulk; they take the SMs the large buckets leave
-  // free), then the remaining whole-SM buckets.
-  std::vector<size_t> launchOrder;
-  launchOrder.reserve(G);
-  if (G > 0) launchOrder.push_back(0);
-  for (size_t gi = 1; gi < G; ++gi)
-    if (B->groups[gi].occupancy > 1) launchOrder.push_back(gi);
-  for (size_t gi = 1; gi < G; ++gi)
-    if (B->groups[gi].occupancy <= 1) launchOrder.push_back(gi);
-  for (size_t gi : launchOrder) {
+  // Launch order: by shared memory per CTA, largest first. The grids are apportioned so that all
+  // of them can be resident at once (partitionGrids); the block scheduler spreads each launch's
+  // CTAs over the SMs with room left, so the largest CTAs must be placed before the small ones
+  // scatter over every SM and leave no SM with room for a large one (first fit, decreasing).
+  std::vector<size_t> launchOrder(G);
+  std::iota(launchOrder.begin(), launchOrder.end(), size_t(0));
+  std::stable_sort(launchOrder.begin(), launchOrder.end(),
+                   [&](size_t a_, size_t b_) { return B->groups[a_].smem > B->groups[b_].smem; });
+  for (size_t rank = 0; rank < G; ++rank) {
+    const size_t gi = launchOrder[rank];
     const Group& g = B->groups[gi];
-    cudaStream_t gs = (G == 1) ? s : B->groupStreams[gi];
+    cudaStream_t gs = (G == 1) ? s : B->groupStreams[rank];
     if (G > 1) CX_CUDA(cudaStreamWaitEvent(gs, B->forkJoin[0], 0));
     LaunchArgs a{};
     a.desc = B->dDesc;
@@ -1320,7 +1404,7 @@ extern "C" int cxg_batch_solve_device_noalloc(cxg_batch* B, double* x, double* s
     a.scratchStride = g.stride;
     a.st = ds;
     a.lay = g.lay;
-    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(g.grid, capDoubles / g.stride));
+    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(g.gridAlone, capDoubles / g.stride));
     CX_CUDA(launchIpm(a, grid, g.block, g.smem, g.fp32, st));
   }
   // history-ordered queues for the next solve, as the other solve entry points keep them (the

@@ -2763,10 +2763,19 @@ static __device__ __noinline__ void adjointInstance(Ctx& c, const LaunchArgs& a)
 // function, while the size-bucket launches of one kernel form ask for different sizes: setting
 // it to each launch's own size left the cap at the last bucket's, below what the earlier nodes of
 // a captured graph carry, and a profiler replaying one of those nodes then failed to launch it.
+// It also asks for the largest shared-memory carveout of the unified L1/shared array. An SM runs
+// CTAs of different kernels side by side only while they share one carveout; with the driver's
+// default choice the small-root forms (a few KB of shared memory) get a smaller carveout than the
+// large ones, so the size buckets launched together could not share SMs and the small buckets
+// started only once whole SMs had drained.
 static inline cudaError_t raiseDynSmem(const void* k, size_t smem) {
   cudaFuncAttributes fa;
   cudaError_t e = cudaFuncGetAttributes(&fa, k);
   if (e != cudaSuccess) return e;
+  if (fa.preferredShmemCarveout != (int)cudaSharedmemCarveoutMaxShared) {
+    e = cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, (int)cudaSharedmemCarveoutMaxShared);
+    if (e != cudaSuccess) return e;
+  }
   if ((int)smem <= fa.maxDynamicSharedSizeBytes) return cudaSuccess;
   return cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 }

@@ -262,3 +262,60 @@ def batch_solve_x(qps, nthreads, settings=None, **kw):
     wall = lib().orc_batch_solve_x(len(qps), arr, C.byref(st), int(nthreads), iptr(stat), iptr(iters), dptr(x),
                                    dptr(s), dptr(z))
     return wall, stat, iters, x, s, z
+
+
+def perturb_q(qp, seed):
+    """A copy of qp whose linear cost q is changed by one unit in the last place in a seeded random
+    direction per entry (q_j (1 +- 2^-52)): a change of the input at the rounding level of FP64."""
+    import dataclasses
+
+    rng = np.random.default_rng(seed)
+    sign = rng.choice(np.array([-1.0, 1.0]), qp.n)
+    return dataclasses.replace(qp, q=np.asarray(qp.q, dtype=np.float64) * (1.0 + sign * 2.0 ** -52))
+
+
+def rounding_ensemble(qps, nthreads, members=4, seed=0, settings=None, **kw):
+    """The oracle's own sensitivity to rounding, per instance: the batch solved as given (the
+    base) and `members` more times with q perturbed by one ulp (perturb_q, seeds seed + 1 ...).
+
+    Returns a dict:
+      base: (statuses, iterations, x, s, z) of the unperturbed solves (concatenated vectors);
+      statuses, iterations: (members + 1, N) arrays, row 0 the base;
+      spread_x, spread_s, spread_z: per instance, the largest max-norm-relative difference
+        max |v_k - v_base| / max(1, max |v_base|) over the members that Solved where the base did
+        (0 where none did);
+      sensitive: per instance, True when the members' statuses differ from the base's or their
+        iteration counts span more than one.
+    Where a one-ulp change of the input moves the reference's own status, iterations or solution,
+    the same movement in another implementation's result is rounding, not a difference in the
+    algorithm."""
+    st = settings if settings is not None else default_settings(**kw)
+    n_off = np.concatenate([[0], np.cumsum([q.n for q in qps])]).astype(np.int64)
+    m_off = np.concatenate([[0], np.cumsum([q.m for q in qps])]).astype(np.int64)
+    runs = [batch_solve_x(qps, nthreads, settings=st)]
+    for k in range(members):
+        runs.append(batch_solve_x([perturb_q(q, seed + 1 + 1000003 * k + i) for i, q in enumerate(qps)], nthreads,
+                                  settings=st))
+    stat = np.stack([r[1] for r in runs]).astype(int)
+    iters = np.stack([r[2] for r in runs]).astype(int)
+    N = len(qps)
+    spreads = {key: np.zeros(N) for key in ("x", "s", "z")}
+    base = runs[0]
+    for key, col, off in (("x", 3, n_off), ("s", 4, m_off), ("z", 5, m_off)):
+        bv = base[col]
+        for r_ in runs[1:]:
+            rv = r_[col]
+            for i in range(N):
+                if stat[0, i] != 1:
+                    continue
+                a, b = off[i], off[i + 1]
+                if b == a:
+                    continue
+                u, v = bv[a:b], rv[a:b]
+                e = float(np.max(np.abs(u - v)) / max(1.0, float(np.max(np.abs(u)))))
+                spreads[key][i] = max(spreads[key][i], e)
+        # members that did not Solve where the base did: their distance is not defined; the
+        # instance is then marked sensitive by its status
+    sensitive = np.any(stat != stat[0], axis=0) | ((iters.max(axis=0) - iters.min(axis=0)) > 1)
+    return {"base": (stat[0], iters[0], base[3], base[4], base[5]), "statuses": stat, "iterations": iters,
+            "spread_x": spreads["x"], "spread_s": spreads["s"], "spread_z": spreads["z"], "sensitive": sensitive}
