@@ -356,6 +356,13 @@ def run_gb300(args, rank, world, local_rank):
         for name, inf_, tx, ts, tz in (("mixed", infos, dx, ds, dz), ("fp64", infos64, dx64, ds64, dz64)):
             gx, gs, gz = (t.cpu().numpy() for t in (tx, ts, tz))
             errors[name] = parity_summary(sample, B, inf_[:len(sample)], cpu_st, cpu_it, (gx, gs, gz), (ox, os_, oz))
+        # the reference against itself: the same sample with q moved at the last bit (oracle.perturb_q),
+        # the scale of rounding-level differences on this family
+        _, pst, pit, px, ps_, pz = orc.batch_solve_x([orc.perturb_q(q_, 1 + i) for i, q_ in enumerate(sample)], ncpu,
+                                                     warm_start=0)
+        pinf = np.zeros(len(sample), dtype=INFO_DTYPE)
+        pinf["status"], pinf["iterations"] = pst, pit
+        errors["oracle_q_last_bit"] = parity_summary(sample, B, pinf, cpu_st, cpu_it, (px, ps_, pz), (ox, os_, oz))
         # ---- roofline of the IPM launch set (one persistent launch per size bucket, run
         # concurrently; timed by CUDA events around the solve on the launching stream) ----
         hbm_peak, peak_kind = peaks()

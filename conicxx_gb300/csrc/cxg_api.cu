@@ -441,7 +441,8 @@ static int buildGroups(cxg_batch* B) {
   scratchTotal = 0;
   for (Group& g : B->groups) {
     g.scratchOff = scratchTotal;
-    scratchTotal += g.stride * g.grid;
+    // the whole-GPU form: only CTA 0 holds the instance, so one scratch region
+    scratchTotal += gridMode ? g.stride : g.stride * g.grid;
   }
   // scratch
   if (B->dScratch) cudaFree(B->dScratch);

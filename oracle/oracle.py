@@ -265,8 +265,9 @@ def batch_solve_x(qps, nthreads, settings=None, **kw):
 
 
 def perturb_q(qp, seed):
-    """A copy of qp whose linear cost q is changed by one unit in the last place in a seeded random
-    direction per entry (q_j (1 +- 2^-52)): a change of the input at the rounding level of FP64."""
+    """A copy of qp whose linear cost q is changed by a relative 2^-52 (one or two units in the
+    last place), in a seeded random direction per entry (q_j (1 +- 2^-52), rounded): a change of
+    the input at the rounding level of FP64."""
     import dataclasses
 
     rng = np.random.default_rng(seed)
@@ -276,7 +277,7 @@ def perturb_q(qp, seed):
 
 def rounding_ensemble(qps, nthreads, members=4, seed=0, settings=None, **kw):
     """The oracle's own sensitivity to rounding, per instance: the batch solved as given (the
-    base) and `members` more times with q perturbed by one ulp (perturb_q, seeds seed + 1 ...).
+    base) and `members` more times with q perturbed at the last bit (perturb_q, seeds seed + 1 ...).
 
     Returns a dict:
       base: (statuses, iterations, x, s, z) of the unperturbed solves (concatenated vectors);
@@ -286,7 +287,7 @@ def rounding_ensemble(qps, nthreads, members=4, seed=0, settings=None, **kw):
         (0 where none did);
       sensitive: per instance, True when the members' statuses differ from the base's or their
         iteration counts span more than one.
-    Where a one-ulp change of the input moves the reference's own status, iterations or solution,
+    Where a last-bit change of the input moves the reference's own status, iterations or solution,
     the same movement in another implementation's result is rounding, not a difference in the
     algorithm."""
     st = settings if settings is not None else default_settings(**kw)

@@ -8,12 +8,14 @@ autograd layer end to end. Gradient vectors are compared by relative 2-norm.
 
 The adjoint is evaluated at the final interior iterate, where the NT scaling still smooths every
 degenerate cone: at the default 1e-8 tolerance it differs from the exact derivative by ~3e-3 on
-the friction-projection problem, identically for the oracle's CPU factorisation and the GPU.
-Two runs stopping at different final iterates therefore agree on such degenerate problems only
-within GRAD_TOL_DEFAULT (FP64) or the sensitivity band GRAD_TOL_BAND (mixed precision), the
-spread of the oracle's own adjoint between stopping tolerances. The tight checks use strictly
-complementary problems (strict_qp), where the adjoint equals the derivative: the GPU adjoint
-matches the oracle's and central finite differences to GRAD_TOL_STRICT there.
+the friction-projection problem, identically for the oracle's CPU factorisation and the GPU. On
+degenerate problems the adjoint at the final iterate therefore moves with the iterate itself:
+on the differentiable-layer problems (configuration 3) the oracle's own adjoint moves by 4-32%
+when q is changed at its last bit (oracle.perturb_q), with the same iteration count. Those
+comparisons are bounded per instance and per gradient by that measured spread
+(oracle_adjoint_with_spread: max(GRAD_TOL, 2 x the spread over six perturbations)). The tight
+checks use strictly complementary problems (strict_qp), where the adjoint equals the derivative:
+the GPU adjoint matches the oracle's and central finite differences to GRAD_TOL_STRICT there.
 """
 import numpy as np
 import pytest
@@ -25,8 +27,33 @@ from conicxx_gb300.problem import QP, Csc
 pytestmark = pytest.mark.gpu
 GRAD_TOL_STRICT = 1e-5  # nondegenerate problems: the adjoint is stable to ~1e-7 across tolerances
 GRAD_TOL = 1e-3
-GRAD_TOL_DEFAULT = 5e-2
-GRAD_TOL_BAND = 0.3
+
+
+def oracle_adjoint_with_spread(oracle_mod, qp, target, members=6):
+    """The oracle's adjoint (dq, db, dP, dA) of L = 1/2 |x - target|^2 at its own solution, and per
+    gradient the largest relative 2-norm change of that adjoint over `members` solves with q
+    changed at its last bit (each at its own solution; members that do not Solve are skipped)."""
+    O = oracle_mod.OracleSolver()
+    assert O.setup(qp, warm_start=0)
+    xo, _, _, io = O.solve()
+    if io["status"] != 1:
+        return None, None
+    go = O.adjoint(xo - target)
+    spread = np.zeros(4)
+    for k in range(members):
+        Ok = oracle_mod.OracleSolver()
+        assert Ok.setup(oracle_mod.perturb_q(qp, 1000 + k), warm_start=0)
+        xk, _, _, ik = Ok.solve()
+        if ik["status"] != 1:
+            continue
+        gk = Ok.adjoint(xk - target)
+        spread = np.maximum(spread, [rel(a, b) for a, b in zip(gk, go)])
+    return go, spread
+
+
+def adjoint_bound(spread):
+    """Per gradient: the rounding-level spread of the oracle's own adjoint, doubled, or GRAD_TOL."""
+    return np.maximum(GRAD_TOL, 2.0 * spread)
 
 
 def strict_qp(seed, n=30, p=5, l=40):
@@ -102,9 +129,8 @@ def test_adjoint_matches_oracle_on_nondegenerate_problems(oracle_mod, precision)
 @pytest.mark.parametrize("precision", [_abi.PRECISION_FP64, _abi.PRECISION_MIXED])
 def test_adjoint_matches_oracle_on_degenerate_layer_problems(oracle_mod, precision):
     """The differentiable-layer problems (n=100, m=150, Zero^10 x R^100_+ x 10 Q^4) are
-    degenerate: the adjoint at the final iterate moves with the iterate itself. Two solvers
-    stopping at different final iterates are therefore compared within GRAD_TOL_DEFAULT (FP64) or
-    the sensitivity band (mixed precision)."""
+    degenerate: the adjoint at the final iterate moves with the iterate itself. Each gradient is
+    compared with the oracle's within twice the oracle's own spread under last-bit changes of q."""
     from conicxx_gb300 import Solver
 
     checked = 0
@@ -112,27 +138,23 @@ def test_adjoint_matches_oracle_on_degenerate_layer_problems(oracle_mod, precisi
         qp = generators.config3_qp(seed)
         t = generators.x_target(seed, qp.n)
         S = Solver()
-        assert S.setup(qp, precision=precision)
+        assert S.setup(qp, precision=precision, warm_start=0)
         sol = S.solve()
-        O = oracle_mod.OracleSolver()
-        assert O.setup(qp)
-        xo, _, _, io = O.solve()
-        assert sol.ok() and io["status"] == 1
+        go, spread = oracle_adjoint_with_spread(oracle_mod, qp, t)
+        assert sol.ok() and go is not None
         g = S.backward(sol.x - t)
-        go = O.adjoint(xo - t)
-        tol = GRAD_TOL_DEFAULT if precision == _abi.PRECISION_FP64 else GRAD_TOL_BAND
-        for name, a, b in zip(("dq", "db", "dP", "dA"), g, go):
-            assert rel(a, b) < tol, (seed, name, rel(a, b))
+        bound = adjoint_bound(spread)
+        for k, (name, a, b) in enumerate(zip(("dq", "db", "dP", "dA"), g, go)):
+            print(seed, name, "device vs oracle %.3e, oracle's own spread %.3e" % (rel(a, b), spread[k]))
+            assert rel(a, b) < bound[k], (seed, name, rel(a, b), spread[k])
         checked += 1
     assert checked == 3
 
 
 def test_batched_adjoint_matches_single_and_oracle(oracle_mod):
     """The batched adjoint equals, per instance, the single-instance Solver's adjoint (the same
-    device computation on the same iterates: tight), and the oracle's within the sensitivity of an
-    adjoint taken at a final interior iterate: between stopping tolerances 1e-8..1e-10 the oracle's
-    own adjoint moves by 5-25% on these degenerate instances, so the oracle comparison bounds the
-    median and the maximum over instances, not each instance tightly."""
+    device computation on the same iterates: tight), and the oracle's within twice the oracle's
+    own spread under last-bit changes of q, per instance and gradient."""
     from conicxx_gb300 import BatchSolver, Solver
 
     qps = [generators.config3_qp(10 + i) for i in range(8)] + [generators.contact_qp(300 + i, cmax=24) for i in range(8)]
@@ -155,16 +177,14 @@ def test_batched_adjoint_matches_single_and_oracle(oracle_mod):
         gs = S.backward(sol.x - targets[i])
         for name, full, ref, sli in zip(("dq", "db", "dP", "dA"), (dq, db, dP, dA), gs, sl):
             assert rel(full[sli], ref) < 1e-9, (i, name, rel(full[sli], ref))
-        O = oracle_mod.OracleSolver()
-        assert O.setup(qp, warm_start=0)
-        xo, _, _, io = O.solve()
-        if io["status"] != 1:
+        go, spread = oracle_adjoint_with_spread(oracle_mod, qp, targets[i])
+        if go is None:
             continue
-        go = O.adjoint(xo - targets[i])
+        bound = adjoint_bound(spread)
+        for k, (full, ref, sli) in enumerate(zip((dq, db, dP, dA), go, sl)):
+            assert rel(full[sli], ref) < bound[k], (i, k, rel(full[sli], ref), spread[k])
         worst.append(max(rel(full[sli], ref) for full, ref, sli in zip((dq, db, dP, dA), go, sl)))
     assert len(worst) >= 12, len(worst)
-    assert np.median(worst) < GRAD_TOL_DEFAULT, worst
-    assert max(worst) < GRAD_TOL_BAND, worst
 
 
 def test_adjoint_against_central_differences(kats, oracle_mod):
@@ -240,13 +260,11 @@ def test_torch_layer_autograd(oracle_mod):
     for got, ref in zip((q.grad, b.grad, Px.grad, Ax.grad), gref):
         assert rel(got.cpu().numpy(), ref) < 1e-12
     for i, qp in enumerate(qps):
-        O = oracle_mod.OracleSolver()
-        assert O.setup(qp, warm_start=0)
-        xo, _, _, io = O.solve()
-        assert io["status"] == 1
-        dq, db, dP, dA = O.adjoint(xo - generators.x_target(i, qp.n))
+        go, spread = oracle_adjoint_with_spread(oracle_mod, qp, generators.x_target(i, qp.n))
+        assert go is not None
+        bound = adjoint_bound(spread)
         s = layer.solver
-        assert rel(q.grad[s.n_off[i]:s.n_off[i + 1]].cpu().numpy(), dq) < GRAD_TOL_DEFAULT
-        assert rel(b.grad[s.m_off[i]:s.m_off[i + 1]].cpu().numpy(), db) < GRAD_TOL_DEFAULT
-        assert rel(Px.grad[s.p_off[i]:s.p_off[i + 1]].cpu().numpy(), dP) < GRAD_TOL_DEFAULT
-        assert rel(Ax.grad[s.a_off[i]:s.a_off[i + 1]].cpu().numpy(), dA) < GRAD_TOL_DEFAULT
+        got = (q.grad[s.n_off[i]:s.n_off[i + 1]], b.grad[s.m_off[i]:s.m_off[i + 1]],
+               Px.grad[s.p_off[i]:s.p_off[i + 1]], Ax.grad[s.a_off[i]:s.a_off[i + 1]])
+        for k, (gv, ref) in enumerate(zip(got, go)):
+            assert rel(gv.cpu().numpy(), ref) < bound[k], (i, k, rel(gv.cpu().numpy(), ref), spread[k])

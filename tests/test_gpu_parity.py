@@ -292,63 +292,91 @@ def test_full_size_contact_batch_properties():
     assert np.all(infos["primal_residual"][ok] < 1e-8) and np.all(infos["dual_residual"][ok] < 1e-8)
 
 
-@pytest.mark.parametrize("precision", [_abi.PRECISION_MIXED, _abi.PRECISION_FP64])
-def test_full_size_contact_batch_agrees_with_oracle(oracle_mod, precision):
-    """The 4096-instance contact batch against the oracle solving the same instances on the host
-    (one thread per instance), compared on every instance:
-    - the same status on >= 99.5% of instances; the rest are listed: borderline instances whose
-      last iterate sits on the 1e-8 threshold, where either solver's rounding decides Solved vs
-      MaxIterations;
-    - on every instance both solve: iterations within +-1 on >= 95%;
-    - x and s within 1e-6 relative (max-norm scaled) on >= 95% and within 1e-4 on all (measured:
-      median 7e-10, 95.5% within 1e-6, max 3e-5). The tail is instances whose stopping iterate
-      differs by an iteration: P = J Minv J' + 1e-6 I is rank deficient up to the 1e-6 shift, so
-      x is determined only to about tol / 1e-6 at the 1e-8 stopping point;
-    - z: wherever it differs from the oracle's by more than 1e-6, the device's (x, s, z) meets the
-      KKT conditions of the original problem to 1e-6 (stationarity, feasibility, s'z), i.e. it
-      is another optimal dual: the duals are not unique on contacts whose normal force vanishes,
-      where the normal row and the friction cone's apex are both active."""
-    _, BatchSolver = _solvers()
+@pytest.fixture(scope="module")
+def contact_ensemble(oracle_mod):
+    """The 4096-instance contact batch on the oracle, as given and with q moved at the last bit in four
+    seeded directions (oracle.rounding_ensemble): the reference's own status, iterations and
+    solution, and how far each moves under a change of the input at the rounding level."""
     qps = generators.contact_batch(4096)
+    E = oracle_mod.rounding_ensemble(qps, os.cpu_count() or 1, members=4, warm_start=0)
+    return qps, E
+
+
+def _max_rel(a, b):
+    return float(np.max(np.abs(a - b)) / max(1.0, float(np.max(np.abs(b))))) if len(b) else 0.0
+
+
+@pytest.mark.parametrize("precision", [_abi.PRECISION_MIXED, _abi.PRECISION_FP64])
+def test_full_size_contact_batch_agrees_with_oracle(contact_ensemble, precision):
+    """The 4096-instance contact batch against the oracle on every instance, measured against the
+    reference's own rounding sensitivity. On this family a last-bit change of q (or compiling the
+    reference with fused multiply-adds) moves the reference's own status on about ten instances,
+    its iteration count by more than one on about 3% and its x beyond 1e-6 on about 5% (measured
+    on the CPU): P = J Minv J' + 1e-6 I is rank deficient up to the shift, many contacts sit at
+    the friction cone's apex with a vanishing normal force, and instances whose last iterates sit
+    at the 1e-8 tolerance are Solved or run to MaxIterations as the rounding falls. An instance is
+    rounding-sensitive when any of four last-bit perturbations of its q changes the oracle's status
+    or moves its iterations by more than one (about 250 of the 4096). Asserted:
+    - status: equal to the oracle's on every instance that is not rounding-sensitive, up to the
+      number of status changes one perturbation alone makes (its mean over the four);
+    - iterations within +-1 on every instance both solve that is not rounding-sensitive, up to 1%
+      of them (the reference built with fused multiply-adds misses this on 0.5%);
+    - x, s and z on every instance both solve: within max(1e-6, 10 x the oracle's own spread over
+      the perturbations) of the oracle's, max-norm relative, or else the device's (x, s, z) is a
+      solution of the original problem of the oracle's quality: stationarity and feasibility
+      within 1e-6 of the data's scale, s'z within 10 x the oracle's own or 1e-7 of the objective.
+      (The reference built with fused multiply-adds needs the second form on 3 instances for x
+      and on 23 for z, whose duals are not unique where a normal force vanishes.)"""
+    _, BatchSolver = _solvers()
+    qps, E = contact_ensemble
     B = BatchSolver(qps, warm_start=0, precision=precision)
     x, s, z, infos = B.solve()
-    st, it = infos["status"], infos["iterations"]
-    _, ost, oit, ox, os_, oz = oracle_mod.batch_solve_x(qps, os.cpu_count() or 1, warm_start=0)
-    agree = st == ost
-    print("status agreement %d/%d, mismatches (index, gpu, oracle):" % (agree.sum(), len(qps)),
-          [(int(i), int(st[i]), int(ost[i])) for i in np.where(~agree)[0]])
-    assert agree.mean() >= 0.995, (agree.sum(), np.where(~agree)[0][:20])
-    both = agree & (st == 1)
-    d = it[both] - oit[both]
-    assert np.mean(np.abs(d) <= 1) >= 0.95, dict(zip(*np.unique(d, return_counts=True)))
+    st, it = infos["status"].astype(int), infos["iterations"].astype(int)
+    ost, oit, ox, os_, oz = E["base"]
+    sens = E["sensitive"]
+    member_flips = [int(np.sum(E["statuses"][k] != ost)) for k in range(1, E["statuses"].shape[0])]
+    mism = np.where(st != ost)[0]
+    outside = [int(i) for i in mism if not sens[i]]
+    print("rounding-sensitive instances: %d; oracle status changes per last-bit perturbation: %s"
+          % (int(sens.sum()), member_flips))
+    print("status mismatches: %d (%d outside the sensitive set: %s)" % (len(mism), len(outside), outside))
+    assert len(outside) <= int(np.ceil(np.mean(member_flips))), outside
+    both = (st == 1) & (ost == 1)
+    d = it - oit
+    ns = both & ~sens
+    bad_it = np.where(ns & (np.abs(d) > 1))[0]
+    print("iterations within +-1 on %d of %d non-sensitive instances both solve; exact on %.4f"
+          % (int(ns.sum()) - len(bad_it), int(ns.sum()), float(np.mean(d[ns] == 0))))
+    assert len(bad_it) <= 0.01 * ns.sum(), bad_it[:20]
     gs, os2 = B.split(x, s, z), B.split(ox, os_, oz)
     errs = {"x": [], "s": [], "z": []}
-    bad_dual = []
+    kkt_route = {"x": [], "s": [], "z": []}
+    failed = []
     for i in np.where(both)[0]:
+        beyond = []
         for k, key in enumerate(("x", "s", "z")):
-            g, o = gs[i][k], os2[i][k]
-            errs[key].append(np.max(np.abs(g - o)) / max(1.0, np.max(np.abs(o))))
-        if errs["z"][-1] > 1e-6:
-            # the device's point is a KKT point of the problem: stationarity and feasibility within
-            # 1e-6 of the data's scale, s'z within 10x the oracle's own s'z or within the relative
-            # gap tolerance (1e-8 of the objective, in the equilibrated space the solver tests;
-            # 1e-7 of it here, unscaled)
-            g_res = qps[i].kkt_residuals(*gs[i])
-            o_res = qps[i].kkt_residuals(*os2[i])
-            scale = max(1.0, np.linalg.norm(qps[i].q), np.linalg.norm(qps[i].b))
-            obj = abs(float(0.5 * gs[i][0] @ sym_upper_matvec(qps[i].P, gs[i][0]) + qps[i].q @ gs[i][0]))
-            ok = (g_res[0] < 1e-6 * scale and g_res[1] < 1e-6 * scale
-                  and abs(g_res[2]) <= max(10.0 * abs(o_res[2]), 1e-7 * max(1.0, obj)))
-            if not ok:
-                bad_dual.append((int(i), g_res, o_res))
-    errs = {k: np.array(v) for k, v in errs.items()}
+            e = _max_rel(gs[i][k], os2[i][k])
+            errs[key].append(e)
+            if e > max(1e-6, 10.0 * E["spread_" + key][i]):
+                beyond.append(key)
+        if not beyond:
+            continue
+        g_res = qps[i].kkt_residuals(*gs[i])
+        o_res = qps[i].kkt_residuals(*os2[i])
+        scale = max(1.0, np.linalg.norm(qps[i].q), np.linalg.norm(qps[i].b))
+        obj = abs(float(0.5 * gs[i][0] @ sym_upper_matvec(qps[i].P, gs[i][0]) + qps[i].q @ gs[i][0]))
+        ok = (g_res[0] < 1e-6 * scale and g_res[1] < 1e-6 * scale
+              and abs(g_res[2]) <= max(10.0 * abs(o_res[2]), 1e-7 * max(1.0, obj)))
+        for key in beyond:
+            kkt_route[key].append(int(i))
+        if not ok:
+            failed.append((int(i), beyond, g_res, o_res))
     for k, v in errs.items():
-        print("%s error vs oracle over %d instances: median %.2e p99 %.2e max %.2e, <= 1e-6: %.4f"
-              % (k, v.size, np.median(v), np.percentile(v, 99), v.max(), np.mean(v <= 1e-6)))
-    for k in ("x", "s"):
-        assert np.mean(errs[k] <= 1e-6) >= 0.95 and errs[k].max() < 1e-4, k
-    print("z beyond 1e-6 of the oracle's on %d instances, each a KKT point of its problem" % np.sum(errs["z"] > 1e-6))
-    assert not bad_dual, bad_dual[:10]
+        v = np.array(v)
+        print("%s vs oracle over %d instances: median %.2e p99 %.2e max %.2e, <= 1e-6: %.4f; beyond the rounding "
+              "bound (checked as KKT points): %d %s" % (k, v.size, np.median(v), np.percentile(v, 99), v.max(),
+                                                       np.mean(v <= 1e-6), len(kkt_route[k]), kkt_route[k][:8]))
+    assert not failed, failed[:10]
 
 
 @pytest.mark.parametrize("precision", [_abi.PRECISION_MIXED, _abi.PRECISION_FP64])

@@ -2,6 +2,8 @@
 
 Each test cites the reference test it re-expresses; tolerances are the reference's.
 """
+import os
+
 import numpy as np
 import pytest
 
@@ -238,3 +240,22 @@ def test_oracle_adjoint_closed_form(oracle_mod, kats):
     assert np.allclose(dq, J @ g, atol=1e-7) and np.allclose(db, [0.5 * g.sum()], atol=1e-7)
     # dL/dP (upper diagonal entries): -(u_i x_i) with u = -dq
     assert np.allclose(dP, -(-dq) * x, atol=1e-7)
+
+
+def test_oracle_rounding_ensemble_moves_statuses():
+    """The rounding ensemble used by the full-batch parity tests: the perturbations of q change each
+    entry by a relative 2^-52 (one or two units in its last place), and on 512 instances of the contact family they move the
+    oracle's own status or iteration count on some instances (the reference's rounding
+    sensitivity the device results are measured against)."""
+    import oracle as orc
+    from conicxx_gb300 import generators
+
+    orc.build()
+    qps = generators.contact_batch(512)
+    q2 = orc.perturb_q(qps[0], 7)
+    assert np.all(np.abs(q2.q - qps[0].q) <= 2.0 * np.spacing(np.abs(qps[0].q)))
+    assert np.any(q2.q != qps[0].q)
+    E = orc.rounding_ensemble(qps, os.cpu_count() or 1, members=2, warm_start=0)
+    assert E["statuses"].shape == (3, 512) and E["spread_x"].shape == (512,)
+    assert E["sensitive"].sum() >= 1
+    assert np.all(E["spread_x"][E["statuses"][0] == 1] < 1e-3)
