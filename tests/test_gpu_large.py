@@ -122,37 +122,69 @@ def _small_large_qp():
     return generators.large_sparse_qp(0, n=1000, m_zero=100, m_nonneg=1200, n_soc=100)
 
 
+def oracle_band(oracle_mod, qp, members=4):
+    """The oracle's solve of qp and its rounding band: the same solve with q changed at its last
+    bit (oracle.perturb_q) `members` times. Returns (x, info, statuses, iterations of every run,
+    largest max-norm-relative change of x over the Solved perturbed runs)."""
+    xo, _, _, io, _ = oracle_mod.solve(qp, warm_start=0)
+    sts, its, spread = [io["status"]], [io["iterations"]], 0.0
+    for k in range(members):
+        xk, _, _, ik, _ = oracle_mod.solve(oracle_mod.perturb_q(qp, 500 + k), warm_start=0)
+        sts.append(ik["status"])
+        its.append(ik["iterations"])
+        if ik["status"] == io["status"] == _abi.STATUS_SOLVED:
+            spread = max(spread, float(np.max(np.abs(xk - xo)) / max(1.0, float(np.max(np.abs(xo))))))
+    return xo, io, sts, its, spread
+
+
+def assert_within_band(sol, band):
+    """Status the oracle's; iterations within one of the oracle's band (its iteration count under
+    last-bit changes of q: on configuration 2's family at n = 1000 it runs 12 to 17 iterations
+    as the rounding falls); x within max(X_TOL, 10 x the band's spread of x)."""
+    xo, io, sts, its, spread = band
+    assert sol.status == io["status"] == _abi.STATUS_SOLVED, (sol.status, sts)
+    assert min(its) - 1 <= sol.info["iterations"] <= max(its) + 1, (sol.info["iterations"], its)
+    assert np.max(np.abs(sol.x - xo)) <= max(X_TOL, 10.0 * spread) * max(1.0, np.max(np.abs(xo))), spread
+
+
+@pytest.fixture(scope="module")
+def small_large_band(oracle_mod):
+    qp = _small_large_qp()
+    return qp, oracle_band(oracle_mod, qp)
+
+
+@pytest.fixture(scope="module")
+def group_lasso_band(oracle_mod):
+    qp = generators.group_lasso_socp(0, groups=60)
+    return qp, oracle_band(oracle_mod, qp)
+
+
 @pytest.mark.parametrize("precision", [_abi.PRECISION_FP64, _abi.PRECISION_MIXED])
-def test_whole_gpu_root_agrees_with_oracle(oracle_mod, precision):
+def test_whole_gpu_root_agrees_with_oracle(small_large_band, precision):
+    """Configuration 2's family at n = 1000 on the whole-GPU root against the oracle's band."""
     from conicxx_gb300 import Solver
 
-    qp = _small_large_qp()
+    qp, band = small_large_band
     S = Solver()
     assert S.setup(qp, precision=precision, warm_start=0, whole_gpu_root=1)
     sol = S.solve()
-    xo, so, zo, io, _ = oracle_mod.solve(qp, warm_start=0)
-    assert sol.status == io["status"] == _abi.STATUS_SOLVED
-    assert abs(sol.info["iterations"] - io["iterations"]) <= 1
-    # both runs stop at the 1e-8 residual/gap tests; what that leaves undetermined in x is larger
-    # here than on the contact instances (P regularised by only 1e-3): measured 1.4e-6 relative
-    assert np.max(np.abs(sol.x - xo)) <= X_TOL * max(1.0, np.max(np.abs(xo)))
+    print("device iterations", sol.info["iterations"], "oracle band", band[3], "x spread %.2e" % band[4])
+    assert_within_band(sol, band)
     st, fe, sz = qp.kkt_residuals(sol.x, sol.s, sol.z)
     assert fe < 1e-6 and sz < 1e-6
 
 
 @pytest.mark.parametrize("precision", [_abi.PRECISION_FP64, _abi.PRECISION_MIXED])
-def test_group_lasso_whole_gpu_agrees_with_oracle(oracle_mod, precision):
+def test_group_lasso_whole_gpu_agrees_with_oracle(group_lasso_band, precision):
     """The block-sparse group-lasso SOCP (60 groups of 16: n = 1020, SOC blocks of dimension 17)."""
     from conicxx_gb300 import Solver
 
-    qp = generators.group_lasso_socp(0, groups=60)
+    qp, band = group_lasso_band
     S = Solver()
     assert S.setup(qp, precision=precision, warm_start=0, whole_gpu_root=1)
     sol = S.solve()
-    xo, _, _, io, _ = oracle_mod.solve(qp, warm_start=0)
-    assert sol.status == io["status"] == _abi.STATUS_SOLVED
-    assert abs(sol.info["iterations"] - io["iterations"]) <= 1
-    assert np.max(np.abs(sol.x - xo)) <= X_TOL * max(1.0, np.max(np.abs(xo)))
+    print("device iterations", sol.info["iterations"], "oracle band", band[3], "x spread %.2e" % band[4])
+    assert_within_band(sol, band)
 
 
 def test_whole_gpu_and_one_cta_forms_agree():
