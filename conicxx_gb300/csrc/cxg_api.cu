@@ -410,6 +410,8 @@ static int buildGroups(cxg_batch* B) {
       D.sVec = o; o += L.vecInSmem ? 0 : vecDoubles(L.nMax, L.mMax, L.nrMax, L.nsocMax);
       D.sVecG = o; o += vecGlobalDoubles(L.mMax);
       D.sKry = o; o += gridMode ? krylovDoubles(L.nMax, L.mMax) : 0;
+      o = r2(o);  // 16-byte aligned: the slices are read by bulk copies
+      D.sSlice = o; o += (gridMode && fp32) ? r2((dfSliceBytes(D.nr) + 7) / 8) : 0;
       D.scratchDoubles = o;
       stride = std::max(stride, o);
     }

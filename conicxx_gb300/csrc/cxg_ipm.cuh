@@ -146,6 +146,7 @@ struct Ctx {
   int* redi;
   double* sc;      // scalar broadcast area
   double* kry;     // whole-GPU form: GMRES Krylov area (krylovDoubles) in scratch
+  unsigned char* slices;  // whole-GPU mixed form: double-float panel slices (dfSliceBytes) in scratch
   GridCtl* grid;   // whole-GPU launch: the root jobs run on every CTA (null: this CTA alone)
 };
 
@@ -1449,6 +1450,227 @@ static __device__ __noinline__ bool tcTrailingStep(float* M, int Tn, int J, long
   return true;
 }
 
+// Double-float trailing update of tile column J on the tensor cores (tcgen05, kind::f16 with BF16
+// operands): the same C_IK -= L_IJ D_J L_KJ^T as superSyrk, by an error-free split of the
+// double-float operands into BF16 slices (the splitting scheme of Ozaki, Ogita, Oishi and Rump,
+// Numer. Algorithms 59, 2012, on BF16 tensor products with FP32 accumulation):
+//  - each row of the 32-wide panels A = L_IJ and B = L_IJ D_J (the double-float product of the
+//    tile routine) is scaled by a power of two 2^-e (e = 1 + the exponent of its largest entry),
+//    so that every entry r lies in [-1, 1], and split as r = a_0 + a_1 + ... + a_5 + rest with
+//    a_s = round(r_s 2^(8 s + 8)) 2^(-8 s - 8), r_0 = r, r_(s+1) = r_s - a_s: each a_s has at most
+//    eight significant bits (a BF16 value), every subtraction is exact (Sterbenz), and the rest
+//    is below 2^-48, the resolution of the double-float value (sliceTile, once per tile, by the
+//    warp that computed it);
+//  - a slice product a_i b_j is an integer multiple of 2^(-8(i + j) - 16) of at most 2^16, so a
+//    sum of 32 of them, and of all pairs of one order i + j, is exact in an FP32 accumulator:
+//    orders 0, 1, 2 accumulate exactly in three 128 x 128 TMEM accumulators, orders 3 to 5 (whose
+//    rounding lies below 2^-48 of the product) in a fourth; the pairs of order 6 and above are
+//    below 2^-48 and left out. 42 MMAs of 128 x 128 x 16 per super-block, issued by one thread;
+//  - the four accumulators are summed in double-float (error-free sums), scaled back by
+//    2^(e_A + e_B) and subtracted from the C tiles in place in global memory.
+// Against the double-float product on the CUDA cores the error bound changes from 2^-48 times the
+// sum of |a_k b_k| to about 2^-46 times (max_k |a_k|)(max_k |b_k|); on quasi-definite roots with
+// pivots spread over 1e20 the factor's componentwise backward error stays near 3e-14 (FP64:
+// 8e-16).
+//
+// Slice area (global, `slices`, dfSliceBytes): for operand o (0 = A, 1 = B), slice s and k-group
+// kg (8 columns), the 16 bytes of root row m at ((o * 6 + s) * 4 + kg) * rows * 16 + m * 16, i.e.
+// each (o, s, kg) plane holds the canonical shared-memory layout of cxg_tc.cuh for every row, so
+// the 128 rows of a super-block are one contiguous copy per plane; then the row exponents, int32,
+// at 768 * rows + (o * rows + m) * 4.
+constexpr int kDfSlices = 6;
+constexpr uint32_t kBf16PanelBytes = (uint32_t)tc::kRows * tc::kPanelK * 2;  // 8 KB
+constexpr uint32_t kDfTmemCols = 512;                                      // four FP32 accumulators
+// one shared-memory buffer: 12 slice panels, then 2 x 128 row exponents
+constexpr uint32_t kDfBufBytes = 2 * kDfSlices * kBf16PanelBytes + 2 * tc::kRows * 4;
+
+// x 2^ex, by one exact multiplication where 2^ex is a normal float (scalbnf otherwise)
+__device__ __forceinline__ float pow2Scale(float x, int ex) {
+  if (ex >= -126 && ex <= 127) return __fmul_rn(x, __int_as_float((ex + 127) << 23));
+  return scalbnf(x, ex);
+}
+
+// Writes the slices (A and B) of the 32 rows of tile (I, J) and their exponents; one warp, lane
+// rr takes row 32 I + rr. L_IJ must be complete in M (written by this warp).
+static __device__ __noinline__ void sliceTile(const df64* M, int Tn, int I, int J, unsigned char* slices) {
+  __syncwarp();
+  const int rr = threadIdx.x & 31;
+  const int64_t rows = (int64_t)Tn * kTile, m = (int64_t)I * kTile + rr;
+  const df64* src = M + tileBase(Tn, I, J) + rr;
+  const df64* Ajj = M + tileBase(Tn, J, J);
+  for (int o = 0; o < 2; ++o) {
+    df64 v[kTile];
+    float mx = 0.0f;
+#pragma unroll
+    for (int k = 0; k < kTile; ++k) {
+      df64 x = src[k * kTileLd];
+      if (o) x = x * Ajj[k * kTileLd + k];
+      v[k] = x;
+      mx = fmaxf(mx, fabsf(x.hi));
+    }
+    const int e = (mx > 0.0f && mx <= 3.0e38f) ? ilogbf(mx) + 1 : 0;
+    reinterpret_cast<int*>(slices + 768 * rows)[o * rows + m] = e;
+#pragma unroll
+    for (int kg = 0; kg < kTile / 8; ++kg) {
+      uint32_t w[kDfSlices][4];
+#pragma unroll
+      for (int t = 0; t < 8; ++t) {
+        float rh = pow2Scale(v[8 * kg + t].hi, -e), rl = pow2Scale(v[8 * kg + t].lo, -e);
+        float p = 256.0f, pinv = 1.0f / 256.0f;
+#pragma unroll
+        for (int sl = 0; sl < kDfSlices; ++sl) {
+          const float as = __fmul_rn(rintf(__fmul_rn(rh, p)), pinv);  // exact: <= 8 significant bits
+          const uint32_t bits = __float_as_uint(as) >> 16;               // its BF16 pattern
+          if (t & 1) w[sl][t >> 1] |= bits << 16;
+          else w[sl][t >> 1] = bits;
+          dfTwoSum(__fsub_rn(rh, as), rl, rh, rl);
+          p = __fmul_rn(p, 256.0f);
+          pinv = __fmul_rn(pinv, 1.0f / 256.0f);
+        }
+      }
+#pragma unroll
+      for (int sl = 0; sl < kDfSlices; ++sl)
+        *reinterpret_cast<uint4*>(slices + ((int64_t)(o * kDfSlices + sl) * 4 + kg) * rows * 16 + m * 16) =
+            make_uint4(w[sl][0], w[sl][1], w[sl][2], w[sl][3]);
+    }
+  }
+}
+
+// The trailing update of step J over the super-blocks this CTA owns (sb = blockIdx.x - 1,
+// + gridDim.x - 1, ...). Software pipeline: the slices of the next super-block arrive by bulk
+// copies (TMA) into the other of two shared-memory buffers while the current super-block's
+// products are taken and its C tiles updated. Shared memory `sm` (128-byte aligned): two buffers
+// of kDfBufBytes. `tmem`: this CTA's 512 accumulator columns; mbarriers: MMA completion and one
+// per buffer, with their phase parities. Returns false when a wait ran out (after waiting once
+// more for the copies and MMAs in flight).
+static __device__ __noinline__ bool tcDfTrailingStep(df64* M, int Tn, int J, long long nsb, const unsigned char* slices,
+                                                     unsigned char* sm, uint32_t tmem, uint32_t mbarMma,
+                                                     uint32_t mbarLd0, uint32_t mbarLd1, uint32_t& phMma,
+                                                     uint32_t& phLd0, uint32_t& phLd1) {
+  const int tid = threadIdx.x;
+  const long long first = (long long)blockIdx.x - 1, stride = (long long)gridDim.x - 1;
+  if (first >= nsb) return true;
+  const int64_t rows = (int64_t)Tn * kTile;
+  const uint32_t bufAddr[2] = {tc::smemAddr(sm), tc::smemAddr(sm) + kDfBufBytes};
+  const uint32_t mbarLd[2] = {mbarLd0, mbarLd1};
+  // thread 0: the slices and exponents of super-block g's A rows (tiles I0 ..) and B rows (K0 ..)
+  auto issueLoads = [&](const SbGeo& g, int buf) {
+    const int nt[2] = {g.ni, g.nk};
+    const int64_t row0[2] = {(int64_t)g.I0 * kTile, (int64_t)g.K0 * kTile};
+    uint32_t bytes = 0;
+    for (int o = 0; o < 2; ++o) bytes += (uint32_t)nt[o] * (kDfSlices * 4 * 512 + 128);
+    tc::mbarArriveExpectTx(mbarLd[buf], bytes);
+    for (int o = 0; o < 2; ++o) {
+      for (int sl = 0; sl < kDfSlices; ++sl)
+        for (int kg = 0; kg < 4; ++kg)
+          tc::bulkLoad(bufAddr[buf] + (uint32_t)(o * kDfSlices + sl) * kBf16PanelBytes + (uint32_t)kg * 2048u,
+                       slices + ((int64_t)(o * kDfSlices + sl) * 4 + kg) * rows * 16 + row0[o] * 16,
+                       (uint32_t)nt[o] * 512u, mbarLd[buf]);
+      tc::bulkLoad(bufAddr[buf] + 2 * kDfSlices * kBf16PanelBytes + (uint32_t)o * tc::kRows * 4,
+                   slices + 768 * rows + (o * rows + row0[o]) * 4, (uint32_t)nt[o] * 128u, mbarLd[buf]);
+    }
+  };
+  if (tid == 0) {
+    tc::fenceProxyAsyncGlobal();  // the slices written this step (generic stores) before the copies
+    issueLoads(sbGeo(first, J, Tn), 0);
+  }
+  int buf = 0;
+  for (long long sb = first; sb < nsb; sb += stride, buf ^= 1) {
+    const SbGeo g = sbGeo(sb, J, Tn);
+    // the next super-block's slices into the other buffer (its previous contents were consumed by
+    // the MMAs and the epilogue of the previous super-block, both complete)
+    if (tid == 0 && sb + stride < nsb) issueLoads(sbGeo(sb + stride, J, Tn), buf ^ 1);
+    uint32_t& phLd = buf ? phLd1 : phLd0;
+    const bool okLd = tc::mbarWait(mbarLd[buf], phLd, kTcWaitNs);
+    phLd ^= 1u;
+    if (!__syncthreads_and(okLd)) {
+      tc::mbarWait(mbarLd[buf ^ 1], buf ? phLd0 : phLd1, kTcWaitNs);
+      __syncthreads();
+      return false;
+    }
+    const int* expA = reinterpret_cast<const int*>(sm + buf * kDfBufBytes + 2 * kDfSlices * kBf16PanelBytes);
+    const int* expB = expA + tc::kRows;
+    // the slice products into four accumulators, by one thread
+    if (tid == 0) {
+      tc::fenceAfterSync();
+      constexpr uint32_t idesc = tc::idescBf16(tc::kRows, tc::kRows);
+      bool used[4] = {false, false, false, false};
+      for (int si = 0; si < kDfSlices; ++si)
+        for (int sj = 0; si + sj < kDfSlices; ++sj) {
+          const int o = min(si + sj, 3);
+          const uint32_t d = tmem + (uint32_t)(o * tc::kRows);
+          const uint32_t aAddr = bufAddr[buf] + (uint32_t)si * kBf16PanelBytes;
+          const uint32_t bAddr = bufAddr[buf] + (uint32_t)(kDfSlices + sj) * kBf16PanelBytes;
+          for (int sK = 0; sK < kTile / 16; ++sK) {
+            const uint32_t off = (uint32_t)sK * 4096u;
+            tc::mmaBf16(d, tc::smemDesc(aAddr + off), tc::smemDesc(bAddr + off), idesc, used[o] || sK > 0);
+          }
+          used[o] = true;
+        }
+      tc::commitTo(mbarMma);
+    }
+    // C -= scaled sum of the accumulators: warp w owns TMEM lanes 32 (w % 4) .. +31 (its rows) and
+    // columns 64 (w / 4) .. +63. All 64 of a thread's C entries are loaded before the MMAs are
+    // waited for (their latency overlaps the products), then updated eight columns at a time.
+    const int warp = tid >> 5, lane = tid & 31;
+    const int q = warp & 3, hh = (warp >> 2) & 1;
+    const int R = 32 * q + lane;
+    const bool rowOk = (R >> 5) < g.ni;
+    // the two C tiles of this thread's columns in row R's tile row (tile columns K0 + 2 hh, + 1)
+    const int64_t colBase0 = tileBase(Tn, g.I0 + (R >> 5), g.K0 + 2 * hh) + (R & 31);
+    const int64_t colBase1 = tileBase(Tn, g.I0 + (R >> 5), g.K0 + 2 * hh + 1) + (R & 31);
+    auto cIdx = [&](int jj) -> int64_t { return ((jj >> 5) ? colBase1 : colBase0) + (jj & 31) * kTileLd; };
+    float ch[64], cl[64];
+#pragma unroll
+    for (int j = 0; j < 64; ++j) {
+      const bool upd = rowOk && sbTile(g, 4 * (R >> 5) + 2 * hh + (j >> 5));
+      const df64 v = upd ? M[cIdx(j)] : df64(0.0f, 0.0f);
+      ch[j] = v.hi;
+      cl[j] = v.lo;
+    }
+    const bool ok = tc::mbarWait(mbarMma, phMma, kTcWaitNs);
+    phMma ^= 1u;
+    tc::fenceAfterSync();
+    if (!__syncthreads_and(ok)) {
+      tc::mbarWait(mbarMma, phMma ^ 1u, kTcWaitNs);  // the MMAs in flight, once more
+      tc::mbarWait(mbarLd[buf ^ 1], buf ? phLd0 : phLd1, kTcWaitNs);
+      __syncthreads();
+      return false;
+    }
+    {
+      const int eR = expA[R];
+      const uint32_t lanes = (uint32_t)(32 * q) << 16;
+#pragma unroll
+      for (int cb = 0; cb < 8; ++cb) {
+        const int c0 = 64 * hh + 8 * cb;
+        float d0[8], d1[8], d2[8], d3[8];
+        tc::tmemLoad8(tmem + lanes + (uint32_t)c0, d0);
+        tc::tmemLoad8(tmem + lanes + (uint32_t)(tc::kRows + c0), d1);
+        tc::tmemLoad8(tmem + lanes + (uint32_t)(2 * tc::kRows + c0), d2);
+        tc::tmemLoad8(tmem + lanes + (uint32_t)(3 * tc::kRows + c0), d3);
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+          const int Cc = c0 + j, jj = 8 * cb + j;
+          if (!(rowOk && sbTile(g, 4 * (R >> 5) + (Cc >> 5)))) continue;
+          float h, e1, h2, e2;
+          dfTwoSum(d0[j], d1[j], h, e1);
+          dfTwoSum(h, d2[j], h2, e2);
+          e1 = __fadd_rn(e1, e2);
+          dfTwoSum(h2, d3[j], h, e2);
+          e1 = __fadd_rn(e1, e2);
+          float sh, sl;
+          dfFastTwoSum(h, e1, sh, sl);
+          const int ex = eR + expB[Cc];
+          M[cIdx(jj)] = df64(ch[jj], cl[jj]) - df64(pow2Scale(sh, ex), pow2Scale(sl, ex));
+        }
+      }
+    }
+    tc::fenceBeforeSync();
+    __syncthreads();  // TMEM read and this buffer consumed before the next super-block
+  }
+  return true;
+}
+
 // Tiled right-looking LDL' of the root over the whole grid. Per tile column J:
 //  (A) the off-diagonal tiles of column J, one warp each; barrier;
 //  (B) the trailing update C_IK -= L_IJ D_J L_KJ^T, J < K <= I, in super-blocks of 4x4 tiles, one
@@ -1466,24 +1688,29 @@ struct TcState {
 
 template <typename T>
 __device__ __noinline__ bool gridLdltSteps(GridCtl* g, int nr, int nx, const DevSettings& st, T* M, PivotStats* ps,
-                                           T* stage, int Tn, int warp, int gw, int GW, bool cta0, TcState& tcs);
+                                           T* stage, unsigned char* slices, int Tn, int warp, int gw, int GW, bool cta0,
+                                           TcState& tcs);
 
+// `slices`: the double-float factor's panel-slice area (dfSliceBytes(nr), 16-byte aligned);
+// unused by the other arithmetics.
 template <typename T>
-__device__ __noinline__ bool gridLdlt(GridCtl* g, int nr, int nx, const DevSettings& st, T* M, PivotStats* ps, T* stage) {
+__device__ __noinline__ bool gridLdlt(GridCtl* g, int nr, int nx, const DevSettings& st, T* M, PivotStats* ps, T* stage,
+                                      unsigned char* slices) {
   const int Tn = rootTiles(nr);
   const int warp = threadIdx.x >> 5, W = blockDim.x >> 5;
   const int gw = (int)blockIdx.x * W + warp, GW = (int)gridDim.x * W;
   const bool cta0 = blockIdx.x == 0;
-  // FP32: the super-blocks go to the tensor cores; every CTA but 0 holds 128 TMEM columns and an
-  // mbarrier for the length of the job
-  constexpr bool kTc = sizeof(T) == 4;
+  // FP32 and double-float: the super-blocks go to the tensor cores; every CTA but 0 holds TMEM
+  // (128 columns for FP32, 512 for double-float) and the mbarriers for the length of the job
+  constexpr bool kTc = ArithOf<T>::v != 0;
+  constexpr uint32_t kCols = (ArithOf<T>::v == 2) ? kDfTmemCols : tc::kTmemCols;
   __shared__ __align__(8) unsigned long long sMbar[3];  // MMA completion, C buffer 0, C buffer 1
   __shared__ uint32_t sTmem;
   TcState tcs{};
   tcs.mbar = tc::smemAddr(&sMbar[0]);
   tcs.stage = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(stage) + 127) & ~static_cast<uintptr_t>(127));
   if (kTc && !cta0) {
-    if (warp == 0) tc::tmemAlloc(tc::smemAddr(&sTmem), tc::kTmemCols);
+    if (warp == 0) tc::tmemAlloc(tc::smemAddr(&sTmem), kCols);
     if (threadIdx.x == 32)
       for (int i = 0; i < 3; ++i) tc::mbarInit(tcs.mbar + 8u * i, 1);
     tc::fenceBeforeSync();
@@ -1491,11 +1718,11 @@ __device__ __noinline__ bool gridLdlt(GridCtl* g, int nr, int nx, const DevSetti
     tc::fenceAfterSync();
     tcs.tmem = sTmem;
   }
-  const bool ok = gridLdltSteps<T>(g, nr, nx, st, M, ps, stage, Tn, warp, gw, GW, cta0, tcs);
+  const bool ok = gridLdltSteps<T>(g, nr, nx, st, M, ps, stage, slices, Tn, warp, gw, GW, cta0, tcs);
   if (kTc && !cta0) {
     tc::fenceBeforeSync();
     __syncthreads();
-    if (warp == 0) tc::tmemDealloc(tcs.tmem, tc::kTmemCols);
+    if (warp == 0) tc::tmemDealloc(tcs.tmem, kCols);
     if (threadIdx.x == 32)
       for (int i = 0; i < 3; ++i) tc::mbarInval(tcs.mbar + 8u * i);
   }
@@ -1504,12 +1731,17 @@ __device__ __noinline__ bool gridLdlt(GridCtl* g, int nr, int nx, const DevSetti
 
 template <typename T>
 __device__ __noinline__ bool gridLdltSteps(GridCtl* g, int nr, int nx, const DevSettings& st, T* M, PivotStats* ps,
-                                           T* stage, int Tn, int warp, int gw, int GW, bool cta0, TcState& tcs) {
+                                           T* stage, unsigned char* slices, int Tn, int warp, int gw, int GW, bool cta0,
+                                           TcState& tcs) {
   if (cta0 && warp == 0) tileFactorDiag<T>(M, 0, nr, nx, st, ps);
   if (!gridSync(g)) return false;
   for (int J = 0; J + 1 < Tn; ++J) {
     T* Ajj = M + tileBase(Tn, J, J);
-    for (int I = J + 1 + gw; I < Tn; I += GW) tileOffDiag<T>(M + tileBase(Tn, I, J), Ajj);
+    for (int I = J + 1 + gw; I < Tn; I += GW) {
+      tileOffDiag<T>(M + tileBase(Tn, I, J), Ajj);
+      // double-float: the warp that finished L_IJ writes its BF16 slices for the trailing update
+      if constexpr (ArithOf<T>::v == 2) sliceTile(M, Tn, I, J, slices);
+    }
     if (!gridSync(g)) return false;
     const int rem = Tn - J - 1;
     const int nb = (rem + 3) >> 2;
@@ -1530,6 +1762,12 @@ __device__ __noinline__ bool gridLdltSteps(GridCtl* g, int nr, int nx, const Dev
     if constexpr (sizeof(T) == 4) {
       if (!tcTrailingStep(M, Tn, J, nsb, tcs.stage, tcs.tmem, tcs.mbar, tcs.mbar + 8u, tcs.mbar + 16u, tcs.phMma,
                           tcs.phLd0, tcs.phLd1)) {
+        if (threadIdx.x == 0) atomicExch(&g->error, 1);
+        return false;
+      }
+    } else if constexpr (ArithOf<T>::v == 2) {
+      if (!tcDfTrailingStep(M, Tn, J, nsb, slices, tcs.stage, tcs.tmem, tcs.mbar, tcs.mbar + 8u, tcs.mbar + 16u,
+                            tcs.phMma, tcs.phLd0, tcs.phLd1)) {
         if (threadIdx.x == 0) atomicExch(&g->error, 1);
         return false;
       }
@@ -1718,7 +1956,7 @@ __device__ bool gridJobT(GridCtl* g, const DevSettings& st, int op, PivotStats* 
   extern __shared__ __align__(16) unsigned char dynSmem[];
   T* stage = reinterpret_cast<T*>(dynSmem + vg->stageOff);
   if (op == kGridOpFactor)
-    return gridAssemble<T>(g, c, st, M, vg->ep, vg->ea) && gridLdlt<T>(g, c.nr, c.n, st, M, ps, stage);
+    return gridAssemble<T>(g, c, st, M, vg->ep, vg->ea) && gridLdlt<T>(g, c.nr, c.n, st, M, ps, stage, c.slices);
   if (op == kGridOpSolve) return gridSolve<T>(g, c.nr, M, reinterpret_cast<T*>(vg->y));
   return false;
 }
@@ -1808,7 +2046,7 @@ __device__ __noinline__ void assembleFactor(Ctx& c, const DevSettings& st, T* M,
     extern __shared__ __align__(16) unsigned char dynSmem[];
     bool ok = gridSync(g) && gridAssemble<T>(g, g->ctx, st, M, ep, ea);
     const long long t2 = (st.record_timings && threadIdx.x == 0) ? clock64() : 0;
-    ok = ok && gridLdlt<T>(g, nr, n, st, M, ps, reinterpret_cast<T*>(dynSmem + g->stageOff));
+    ok = ok && gridLdlt<T>(g, nr, n, st, M, ps, reinterpret_cast<T*>(dynSmem + g->stageOff), c.slices);
     __syncthreads();
     const bool regularized = st.linear_solver == 2;
     fail = !ok ? 1 : (regularized ? (((double)ps->nreg > 0.05 * (double)nr) ? 1 : 0) : ps->zero);
@@ -2635,6 +2873,7 @@ static __device__ void setupCtx(Ctx& c, const LaunchArgs& a, int inst, unsigned 
   c.red = reinterpret_cast<double*>(smem + L.redOff);
   c.sc = c.red + 128;
   c.kry = scratch + D.sKry;
+  c.slices = reinterpret_cast<unsigned char*>(scratch + D.sSlice);
   c.redi = sRedi;
   c.grid = nullptr;
 }

@@ -76,7 +76,7 @@ template <typename T>
 __global__ void __launch_bounds__(256, 1) denseProbeGridKernel(int nr, int nx, const double* K, const double* b,
                                                                DevSettings st, T* M, T* y, GridCtl* g, double* Lout,
                                                                double* Dout, double* xout, long long* cyc,
-                                                               int* flags) {
+                                                               int* flags, unsigned char* slices) {
   __shared__ PivotStats sPs;
   extern __shared__ __align__(16) unsigned char stageSmem[];
   T* stage = reinterpret_cast<T*>(stageSmem);
@@ -100,7 +100,7 @@ __global__ void __launch_bounds__(256, 1) denseProbeGridKernel(int nr, int nx, c
   for (int64_t i = gt; i < (int64_t)Tn * kTile; i += gs) y[i] = (i < nr) ? (T)b[i] : (T)0;
   ok = ok && gridSync(g);
   const unsigned long long t0 = globalNs();
-  ok = ok && gridLdlt<T>(g, nr, nx, st, M, &sPs, stage);
+  ok = ok && gridLdlt<T>(g, nr, nx, st, M, &sPs, stage, slices);
   const unsigned long long t1 = globalNs();
   for (int64_t t = gt; t < nn; t += gs) {
     const int i = (int)(t % nr), j = (int)(t / nr);
@@ -136,7 +136,9 @@ static cudaError_t probeGridLaunch(int nr, int nx, const double* K, const double
   if (occ * numSM < 2) return cudaErrorInvalidConfiguration;
   T *M = nullptr, *y = nullptr;
   GridCtl* g = nullptr;
+  unsigned char* slices = nullptr;  // double-float: the panel slices of the tensor-core trailing update
   e = cudaMalloc((void**)&M, (size_t)rootSize(nr) * sizeof(T));
+  if (e == cudaSuccess && ArithOf<T>::v == 2) e = cudaMalloc((void**)&slices, (size_t)dfSliceBytes(nr));
   if (e == cudaSuccess) e = cudaMalloc((void**)&y, (size_t)rootTiles(nr) * kTile * sizeof(T));
   if (e == cudaSuccess) e = cudaMalloc((void**)&g, sizeof(GridCtl));
   if (e == cudaSuccess) e = cudaMemset(g, 0, sizeof(GridCtl));
@@ -144,7 +146,7 @@ static cudaError_t probeGridLaunch(int nr, int nx, const double* K, const double
     int nrv = nr, nxv = nx;
     DevSettings stv = st;
     void* args[] = {&nrv, &nxv, (void*)&K, (void*)&b, &stv, (void*)&M, (void*)&y, (void*)&g,
-                    (void*)&L, (void*)&D, (void*)&x, (void*)&cyc, (void*)&flags};
+                    (void*)&L, (void*)&D, (void*)&x, (void*)&cyc, (void*)&flags, (void*)&slices};
     e = cudaLaunchCooperativeKernel((const void*)denseProbeGridKernel<T>, dim3(occ * numSM), dim3(256), args, smem,
                                     nullptr);
     if (e == cudaSuccess) e = cudaDeviceSynchronize();
@@ -152,6 +154,7 @@ static cudaError_t probeGridLaunch(int nr, int nx, const double* K, const double
   if (M) cudaFree(M);
   if (y) cudaFree(y);
   if (g) cudaFree(g);
+  if (slices) cudaFree(slices);
   return e;
 }
 

@@ -86,6 +86,7 @@ struct InstanceDesc {
   int64_t sVec;                       // FP64 vectors that do not fit in shared memory
   int64_t sVecG;                      // FP64 vectors always kept in scratch (vecGlobalDoubles)
   int64_t sKry;                       // whole-GPU form: the GMRES Krylov area (krylovDoubles)
+  int64_t sSlice;                     // whole-GPU mixed form: the double-float panel slices (dfSliceBytes)
   int64_t scratchDoubles;             // total per-CTA scratch this instance needs
   int64_t bwdOff;                     // offset of this instance's saved final state (differentiable)
   double cost;                        // scheduling weight (~ nr^3)

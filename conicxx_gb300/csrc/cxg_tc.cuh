@@ -1,6 +1,7 @@
 // Blackwell tensor-core helpers (sm_103a): tcgen05 MMA with operands in shared memory and the
-// accumulator in tensor memory (TMEM), written as inline PTX, and the FP32 trailing update of the
-// whole-GPU root factor built on them.
+// accumulator in tensor memory (TMEM), written as inline PTX, on which the whole-GPU root
+// factor's FP32 (kind::tf32) and double-float (kind::f16 with BF16 slices) trailing updates are
+// built.
 //
 // Operand layout: the "K-major, no swizzle" canonical layout of the tcgen05 shared-memory matrix
 // descriptor. A 128-row x 32-column TF32 panel is stored as core matrices of 8 rows x 16 bytes
@@ -10,6 +11,10 @@
 // offset) and adjacent 8-row groups 128 bytes apart (its stride-dimension byte offset). One
 // kind::tf32 MMA consumes K = 8 (two core-matrix columns): the MMA over columns 8s .. 8s+7
 // starts at byte 4096 s of the panel. A panel is 16 KB.
+//
+// The same byte layout holds a 128 x 32 BF16 panel as 8 x 8-value core matrices: element (m, k) at
+//     (k / 8) * 2048 + (m / 8) * 128 + (m % 8) * 16 + (k % 8) * 2,
+// 8 KB per panel, one kind::f16 MMA (K = 16) per 4096 bytes.
 //
 // D[128 x 128] (+)= A[128 x 8] B[128 x 8]^T accumulates in FP32 in 128 TMEM columns: row i of D in
 // TMEM lane i, column j in column base + j. A warp reads only the 32 lanes of its quarter
@@ -53,6 +58,13 @@ __host__ __device__ constexpr uint32_t idescTf32(int M, int N) {
   return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
 }
 
+// Instruction descriptor of kind::f16 with BF16 A and B: D in FP32 (bits 4-5 = 1), A and B BF16
+// (bits 7-9 and 10-12 = 1), both K-major, N >> 3 in bits 17-22, M >> 4 in bits 24-28. One MMA
+// consumes K = 16 (two core-matrix columns of 8 BF16 values each).
+__host__ __device__ constexpr uint32_t idescBf16(int M, int N) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
 // round to TF32 (nearest, ties away from zero), kept as an FP32 bit pattern
 __device__ __forceinline__ float toTf32(float x) {
   uint32_t r;
@@ -65,6 +77,15 @@ __device__ __forceinline__ void mmaTf32(uint32_t dTmem, uint64_t aDesc, uint64_t
   asm volatile(
       "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
       "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(dTmem),
+      "l"(aDesc), "l"(bDesc), "r"(idesc), "r"(accumulate ? 1u : 0u)
+      : "memory");
+}
+
+// D[tmem] (+)= A B^T with BF16 operands, FP32 accumulation; issued by one thread
+__device__ __forceinline__ void mmaBf16(uint32_t dTmem, uint64_t aDesc, uint64_t bDesc, uint32_t idesc, bool accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(dTmem),
       "l"(aDesc), "l"(bDesc), "r"(idesc), "r"(accumulate ? 1u : 0u)
       : "memory");
 }
@@ -142,6 +163,18 @@ __device__ __forceinline__ void bulkWaitRead0() { asm volatile("cp.async.bulk.wa
 // ... and are complete in global memory
 __device__ __forceinline__ void bulkWait0() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
 __device__ __forceinline__ void fenceProxyAsyncGlobal() { asm volatile("fence.proxy.async.global;" ::: "memory"); }
+
+// 8 consecutive TMEM columns of this thread's lane (warp quarter) into registers
+__device__ __forceinline__ void tmemLoad8(uint32_t taddr, float (&v)[8]) {
+  uint32_t r[8];
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+               : "r"(taddr)
+               : "memory");
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(r[i]);
+}
 
 // 16 consecutive TMEM columns of this thread's lane (warp quarter) into registers
 __device__ __forceinline__ void tmemLoad16(uint32_t taddr, float (&v)[16]) {
