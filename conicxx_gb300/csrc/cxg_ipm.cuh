@@ -1643,25 +1643,26 @@ static __device__ __noinline__ bool tcDfTrailingStep(df64* M, int Tn, int J, lon
 #pragma unroll
       for (int cb = 0; cb < 8; ++cb) {
         const int c0 = 64 * hh + 8 * cb;
-        float d0[8], d1[8], d2[8], d3[8];
-        tc::tmemLoad8(tmem + lanes + (uint32_t)c0, d0);
-        tc::tmemLoad8(tmem + lanes + (uint32_t)(tc::kRows + c0), d1);
-        tc::tmemLoad8(tmem + lanes + (uint32_t)(2 * tc::kRows + c0), d2);
-        tc::tmemLoad8(tmem + lanes + (uint32_t)(3 * tc::kRows + c0), d3);
+        float d[4][8];
+        tc::tmemLoad8x4(tmem + lanes + (uint32_t)c0, (uint32_t)tc::kRows, d);
+        // branch-free over the eight entries (independent chains); only the stores are predicated
 #pragma unroll
         for (int j = 0; j < 8; ++j) {
           const int Cc = c0 + j, jj = 8 * cb + j;
-          if (!(rowOk && sbTile(g, 4 * (R >> 5) + (Cc >> 5)))) continue;
           float h, e1, h2, e2;
-          dfTwoSum(d0[j], d1[j], h, e1);
-          dfTwoSum(h, d2[j], h2, e2);
+          dfTwoSum(d[0][j], d[1][j], h, e1);
+          dfTwoSum(h, d[2][j], h2, e2);
           e1 = __fadd_rn(e1, e2);
-          dfTwoSum(h2, d3[j], h, e2);
+          dfTwoSum(h2, d[3][j], h, e2);
           e1 = __fadd_rn(e1, e2);
           float sh, sl;
           dfFastTwoSum(h, e1, sh, sl);
+          // x 2^(eR + eB) as two exact power-of-two factors, each within the normal range
           const int ex = eR + expB[Cc];
-          M[cIdx(jj)] = df64(ch[jj], cl[jj]) - df64(pow2Scale(sh, ex), pow2Scale(sl, ex));
+          const int ex1 = min(max(ex >> 1, -126), 127), ex2 = min(max(ex - (ex >> 1), -126), 127);
+          const float f1 = __int_as_float((ex1 + 127) << 23), f2 = __int_as_float((ex2 + 127) << 23);
+          const df64 r = df64(ch[jj], cl[jj]) - df64(__fmul_rn(__fmul_rn(sh, f1), f2), __fmul_rn(__fmul_rn(sl, f1), f2));
+          if (rowOk && sbTile(g, 4 * (R >> 5) + (Cc >> 5))) M[cIdx(jj)] = r;
         }
       }
     }

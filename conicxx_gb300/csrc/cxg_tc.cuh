@@ -176,6 +176,24 @@ __device__ __forceinline__ void tmemLoad8(uint32_t taddr, float (&v)[8]) {
   for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(r[i]);
 }
 
+// 8 consecutive TMEM columns of this thread's lane at each of four column offsets (accumulators),
+// with one wait for all four loads
+__device__ __forceinline__ void tmemLoad8x4(uint32_t taddr, uint32_t accStride, float (&v)[4][8]) {
+  uint32_t r[4][8];
+#pragma unroll
+  for (int a = 0; a < 4; ++a)
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+                 : "=r"(r[a][0]), "=r"(r[a][1]), "=r"(r[a][2]), "=r"(r[a][3]), "=r"(r[a][4]), "=r"(r[a][5]),
+                   "=r"(r[a][6]), "=r"(r[a][7])
+                 : "r"(taddr + (uint32_t)a * accStride)
+                 : "memory");
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int a = 0; a < 4; ++a)
+#pragma unroll
+    for (int i = 0; i < 8; ++i) v[a][i] = __uint_as_float(r[a][i]);
+}
+
 // 16 consecutive TMEM columns of this thread's lane (warp quarter) into registers
 __device__ __forceinline__ void tmemLoad16(uint32_t taddr, float (&v)[16]) {
   uint32_t r[16];
