@@ -1450,39 +1450,51 @@ static __device__ __noinline__ bool tcTrailingStep(float* M, int Tn, int J, long
   return true;
 }
 
-// Double-float trailing update of tile column J on the tensor cores (tcgen05, kind::f16 with BF16
-// operands): the same C_IK -= L_IJ D_J L_KJ^T as superSyrk, by an error-free split of the
-// double-float operands into BF16 slices (the splitting scheme of Ozaki, Ogita, Oishi and Rump,
-// Numer. Algorithms 59, 2012, on BF16 tensor products with FP32 accumulation):
-//  - each row of the 32-wide panels A = L_IJ and B = L_IJ D_J (the double-float product of the
-//    tile routine) is scaled by a power of two 2^-e (e = 1 + the exponent of its largest entry),
-//    so that every entry r lies in [-1, 1], and split as r = a_0 + a_1 + ... + a_5 + rest with
-//    a_s = round(r_s 2^(8 s + 8)) 2^(-8 s - 8), r_0 = r, r_(s+1) = r_s - a_s: each a_s has at most
-//    eight significant bits (a BF16 value), every subtraction is exact (Sterbenz), and the rest
-//    is below 2^-48, the resolution of the double-float value (sliceTile, once per tile, by the
-//    warp that computed it);
+// tensor-core state of a CTA for the length of one factorisation job
+struct TcState {
+  unsigned char* stage;  // kGridTcStageBytes, 128-byte aligned
+  uint32_t tmem, mbar;   // TMEM base; three mbarriers at mbar, mbar + 8, mbar + 16
+  uint32_t phMma, phLd0, phLd1;
+};
+
+// Double-float trailing update on the tensor cores (tcgen05, kind::f16 with BF16 operands), over a
+// pair of tile columns (J0, J0 + 1) at once: C_IK -= L_I,pair D_pair L_K,pair^T, K = 64, by an
+// error-free split of the double-float operands into BF16 slices (the splitting scheme of Ozaki,
+// Ogita, Oishi and Rump, Numer. Algorithms 59, 2012, on BF16 tensor products with FP32
+// accumulation):
+//  - each 64-wide row of the panels A = [L_I,J0 L_I,J0+1] and B = A D (the double-float products
+//    of the tile routine) is scaled by a power of two 2^-e (e = 1 + the exponent of its largest
+//    entry), so that every entry r lies in [-1, 1], and split as r = a_0 + a_1 + ... + a_5 + rest
+//    with a_s = round(r_s 2^(8 s + 8)) 2^(-8 s - 8), r_0 = r, r_(s+1) = r_s - a_s: each a_s has at
+//    most eight significant bits (a BF16 value), every subtraction is exact (Sterbenz), and the
+//    rest is below 2^-48, the resolution of the double-float value (sliceRowPair, once per tile
+//    row, by the warp that computed the row's second tile);
 //  - a slice product a_i b_j is an integer multiple of 2^(-8(i + j) - 16) of at most 2^16, so a
-//    sum of 32 of them, and of all pairs of one order i + j, is exact in an FP32 accumulator:
-//    orders 0, 1, 2 accumulate exactly in three 128 x 128 TMEM accumulators, orders 3 to 5 (whose
-//    rounding lies below 2^-48 of the product) in a fourth; the pairs of order 6 and above are
-//    below 2^-48 and left out. 42 MMAs of 128 x 128 x 16 per super-block, issued by one thread;
+//    sum of 64 of them over one, two or three pairs of one order i + j stays below 2^24, exact in
+//    an FP32 accumulator: orders 0, 1, 2 accumulate exactly in three 128 x 128 TMEM accumulators,
+//    orders 3 to 5 (whose rounding lies below 2^-48 of the product) in a fourth; the pairs of
+//    order 6 and above are below 2^-48 and left out. 84 MMAs of 128 x 128 x 16 per super-block,
+//    issued by one thread;
 //  - the four accumulators are summed in double-float (error-free sums), scaled back by
 //    2^(e_A + e_B) and subtracted from the C tiles in place in global memory.
 // Against the double-float product on the CUDA cores the error bound changes from 2^-48 times the
-// sum of |a_k b_k| to about 2^-46 times (max_k |a_k|)(max_k |b_k|); on quasi-definite roots with
+// sum of |a_k b_k| to about 2^-45 times (max_k |a_k|)(max_k |b_k|); on quasi-definite roots with
 // pivots spread over 1e20 the factor's componentwise backward error stays near 3e-14 (FP64:
 // 8e-16).
 //
 // Slice area (global, `slices`, dfSliceBytes): for operand o (0 = A, 1 = B), slice s and k-group
-// kg (8 columns), the 16 bytes of root row m at ((o * 6 + s) * 4 + kg) * rows * 16 + m * 16, i.e.
-// each (o, s, kg) plane holds the canonical shared-memory layout of cxg_tc.cuh for every row, so
-// the 128 rows of a super-block are one contiguous copy per plane; then the row exponents, int32,
-// at 768 * rows + (o * rows + m) * 4.
+// kg (8 of the 64 columns), the 16 bytes of root row m at ((o * 6 + s) * 8 + kg) * rows * 16 +
+// m * 16, i.e. each (o, s, kg) plane holds the canonical shared-memory layout of cxg_tc.cuh for
+// every row, so the 128 rows of a super-block are one contiguous copy per plane; then the row
+// exponents, int32, at 1536 * rows + (o * rows + m) * 4.
 constexpr int kDfSlices = 6;
-constexpr uint32_t kBf16PanelBytes = (uint32_t)tc::kRows * tc::kPanelK * 2;  // 8 KB
-constexpr uint32_t kDfTmemCols = 512;                                      // four FP32 accumulators
-// one shared-memory buffer: 12 slice panels, then 2 x 128 row exponents
-constexpr uint32_t kDfBufBytes = 2 * kDfSlices * kBf16PanelBytes + 2 * tc::kRows * 4;
+constexpr int kDfK = 2 * kTile;                                          // columns per C visit
+constexpr uint32_t kDfPanelBytes = (uint32_t)tc::kRows * kDfK * 2;       // 16 KB: 128 x 64 BF16
+constexpr uint32_t kDfTmemCols = 512;                                    // four FP32 accumulators
+constexpr uint32_t kDfOpBytes = 2 * kDfSlices * kDfPanelBytes;           // 192 KB of operands
+constexpr uint32_t kDfExpBytes = 2 * tc::kRows * 4;                      // row exponents, A and B
+constexpr int64_t kDfStageBytes = (int64_t)kDfOpBytes + 2 * kDfExpBytes; // one operand + two exponent buffers
+static_assert(kDfStageBytes + 128 <= kGridTcStageBytes, "double-float staging exceeds the stage area");
 
 // x 2^ex, by one exact multiplication where 2^ex is a normal float (scalbnf otherwise)
 __device__ __forceinline__ float pow2Scale(float x, int ex) {
@@ -1490,32 +1502,34 @@ __device__ __forceinline__ float pow2Scale(float x, int ex) {
   return scalbnf(x, ex);
 }
 
-// Writes the slices (A and B) of the 32 rows of tile (I, J) and their exponents; one warp, lane
-// rr takes row 32 I + rr. L_IJ must be complete in M (written by this warp).
-static __device__ __noinline__ void sliceTile(const df64* M, int Tn, int I, int J, unsigned char* slices) {
+// Writes the slices (A and B) of the 32 rows of tile row I over the tile columns J0, J0 + 1 and
+// their exponents; one warp, lane rr takes row 32 I + rr. L_I,J0 and L_I,J0+1 must be complete
+// in M (the second written by this warp, the first before the last grid barrier).
+static __device__ __noinline__ void sliceRowPair(const df64* M, int Tn, int I, int J0, unsigned char* slices) {
   __syncwarp();
   const int rr = threadIdx.x & 31;
   const int64_t rows = (int64_t)Tn * kTile, m = (int64_t)I * kTile + rr;
-  const df64* src = M + tileBase(Tn, I, J) + rr;
-  const df64* Ajj = M + tileBase(Tn, J, J);
+  const df64* src[2] = {M + tileBase(Tn, I, J0) + rr, M + tileBase(Tn, I, J0 + 1) + rr};
+  const df64* dg[2] = {M + tileBase(Tn, J0, J0), M + tileBase(Tn, J0 + 1, J0 + 1)};
   for (int o = 0; o < 2; ++o) {
-    df64 v[kTile];
+    auto value = [&](int k) -> df64 {
+      const int t = k >> 5, kk = k & 31;
+      df64 x = src[t][kk * kTileLd];
+      if (o) x = x * dg[t][kk * kTileLd + kk];
+      return x;
+    };
     float mx = 0.0f;
-#pragma unroll
-    for (int k = 0; k < kTile; ++k) {
-      df64 x = src[k * kTileLd];
-      if (o) x = x * Ajj[k * kTileLd + k];
-      v[k] = x;
-      mx = fmaxf(mx, fabsf(x.hi));
-    }
+#pragma unroll 8
+    for (int k = 0; k < kDfK; ++k) mx = fmaxf(mx, fabsf(value(k).hi));
     const int e = (mx > 0.0f && mx <= 3.0e38f) ? ilogbf(mx) + 1 : 0;
-    reinterpret_cast<int*>(slices + 768 * rows)[o * rows + m] = e;
-#pragma unroll
-    for (int kg = 0; kg < kTile / 8; ++kg) {
+    reinterpret_cast<int*>(slices + 1536 * rows)[o * rows + m] = e;
+#pragma unroll 1
+    for (int kg = 0; kg < kDfK / 8; ++kg) {
       uint32_t w[kDfSlices][4];
 #pragma unroll
       for (int t = 0; t < 8; ++t) {
-        float rh = pow2Scale(v[8 * kg + t].hi, -e), rl = pow2Scale(v[8 * kg + t].lo, -e);
+        const df64 v = value(8 * kg + t);
+        float rh = pow2Scale(v.hi, -e), rl = pow2Scale(v.lo, -e);
         float p = 256.0f, pinv = 1.0f / 256.0f;
 #pragma unroll
         for (int sl = 0; sl < kDfSlices; ++sl) {
@@ -1530,66 +1544,63 @@ static __device__ __noinline__ void sliceTile(const df64* M, int Tn, int I, int 
       }
 #pragma unroll
       for (int sl = 0; sl < kDfSlices; ++sl)
-        *reinterpret_cast<uint4*>(slices + ((int64_t)(o * kDfSlices + sl) * 4 + kg) * rows * 16 + m * 16) =
+        *reinterpret_cast<uint4*>(slices + ((int64_t)(o * kDfSlices + sl) * (kDfK / 8) + kg) * rows * 16 + m * 16) =
             make_uint4(w[sl][0], w[sl][1], w[sl][2], w[sl][3]);
     }
   }
 }
 
-// The trailing update of step J over the super-blocks this CTA owns (sb = blockIdx.x - 1,
-// + gridDim.x - 1, ...). Software pipeline: the slices of the next super-block arrive by bulk
-// copies (TMA) into the other of two shared-memory buffers while the current super-block's
-// products are taken and its C tiles updated. Shared memory `sm` (128-byte aligned): two buffers
-// of kDfBufBytes. `tmem`: this CTA's 512 accumulator columns; mbarriers: MMA completion and one
-// per buffer, with their phase parities. Returns false when a wait ran out (after waiting once
-// more for the copies and MMAs in flight).
+// The trailing update of column pair (J - 1, J) over the super-blocks this CTA owns (sb =
+// blockIdx.x - 1, + gridDim.x - 1, ...; tile rows and columns from J + 1). Pipeline: a
+// super-block's slices and exponents arrive by bulk copies (TMA); its 84 MMAs run; meanwhile its
+// 64 C entries per thread are loaded into registers; once the MMAs are complete the next
+// super-block's copies are issued (the operand buffer is free; the exponents alternate between
+// two buffers) and overlap this super-block's C update. Shared memory `sm` (128-byte aligned):
+// kDfStageBytes. `tmem`: this CTA's 512 accumulator columns; mbarriers: MMA completion and
+// copies, with their phase parities. Returns false when a wait ran out (after waiting once more
+// for the copies and MMAs in flight).
 static __device__ __noinline__ bool tcDfTrailingStep(df64* M, int Tn, int J, long long nsb, const unsigned char* slices,
                                                      unsigned char* sm, uint32_t tmem, uint32_t mbarMma,
-                                                     uint32_t mbarLd0, uint32_t mbarLd1, uint32_t& phMma,
-                                                     uint32_t& phLd0, uint32_t& phLd1) {
+                                                     uint32_t mbarLd, uint32_t& phMma, uint32_t& phLd) {
   const int tid = threadIdx.x;
   const long long first = (long long)blockIdx.x - 1, stride = (long long)gridDim.x - 1;
   if (first >= nsb) return true;
   const int64_t rows = (int64_t)Tn * kTile;
-  const uint32_t bufAddr[2] = {tc::smemAddr(sm), tc::smemAddr(sm) + kDfBufBytes};
-  const uint32_t mbarLd[2] = {mbarLd0, mbarLd1};
-  // thread 0: the slices and exponents of super-block g's A rows (tiles I0 ..) and B rows (K0 ..)
-  auto issueLoads = [&](const SbGeo& g, int buf) {
+  const uint32_t opAddr = tc::smemAddr(sm);
+  const uint32_t expAddr[2] = {opAddr + kDfOpBytes, opAddr + kDfOpBytes + kDfExpBytes};
+  constexpr int kPlanes = kDfSlices * (kDfK / 8);  // per operand
+  // thread 0: the slices of super-block g's A rows (tiles I0 ..) and B rows (K0 ..), exponents
+  // into exponent buffer eb
+  auto issueLoads = [&](const SbGeo& g, int eb) {
     const int nt[2] = {g.ni, g.nk};
     const int64_t row0[2] = {(int64_t)g.I0 * kTile, (int64_t)g.K0 * kTile};
     uint32_t bytes = 0;
-    for (int o = 0; o < 2; ++o) bytes += (uint32_t)nt[o] * (kDfSlices * 4 * 512 + 128);
-    tc::mbarArriveExpectTx(mbarLd[buf], bytes);
+    for (int o = 0; o < 2; ++o) bytes += (uint32_t)nt[o] * (kPlanes * 512 + 128);
+    tc::mbarArriveExpectTx(mbarLd, bytes);
     for (int o = 0; o < 2; ++o) {
       for (int sl = 0; sl < kDfSlices; ++sl)
-        for (int kg = 0; kg < 4; ++kg)
-          tc::bulkLoad(bufAddr[buf] + (uint32_t)(o * kDfSlices + sl) * kBf16PanelBytes + (uint32_t)kg * 2048u,
-                       slices + ((int64_t)(o * kDfSlices + sl) * 4 + kg) * rows * 16 + row0[o] * 16,
-                       (uint32_t)nt[o] * 512u, mbarLd[buf]);
-      tc::bulkLoad(bufAddr[buf] + 2 * kDfSlices * kBf16PanelBytes + (uint32_t)o * tc::kRows * 4,
-                   slices + 768 * rows + (o * rows + row0[o]) * 4, (uint32_t)nt[o] * 128u, mbarLd[buf]);
+        for (int kg = 0; kg < kDfK / 8; ++kg)
+          tc::bulkLoad(opAddr + (uint32_t)(o * kDfSlices + sl) * kDfPanelBytes + (uint32_t)kg * 2048u,
+                       slices + ((int64_t)(o * kDfSlices + sl) * (kDfK / 8) + kg) * rows * 16 + row0[o] * 16,
+                       (uint32_t)nt[o] * 512u, mbarLd);
+      tc::bulkLoad(expAddr[eb] + (uint32_t)o * tc::kRows * 4, slices + 1536 * rows + (o * rows + row0[o]) * 4,
+                   (uint32_t)nt[o] * 128u, mbarLd);
     }
   };
   if (tid == 0) {
     tc::fenceProxyAsyncGlobal();  // the slices written this step (generic stores) before the copies
     issueLoads(sbGeo(first, J, Tn), 0);
   }
-  int buf = 0;
-  for (long long sb = first; sb < nsb; sb += stride, buf ^= 1) {
+  int eb = 0;
+  for (long long sb = first; sb < nsb; sb += stride, eb ^= 1) {
     const SbGeo g = sbGeo(sb, J, Tn);
-    // the next super-block's slices into the other buffer (its previous contents were consumed by
-    // the MMAs and the epilogue of the previous super-block, both complete)
-    if (tid == 0 && sb + stride < nsb) issueLoads(sbGeo(sb + stride, J, Tn), buf ^ 1);
-    uint32_t& phLd = buf ? phLd1 : phLd0;
-    const bool okLd = tc::mbarWait(mbarLd[buf], phLd, kTcWaitNs);
+    const bool okLd = tc::mbarWait(mbarLd, phLd, kTcWaitNs);
     phLd ^= 1u;
     if (!__syncthreads_and(okLd)) {
-      tc::mbarWait(mbarLd[buf ^ 1], buf ? phLd0 : phLd1, kTcWaitNs);
+      tc::mbarWait(mbarLd, phLd ^ 1u, kTcWaitNs);  // the copies in flight, once more
       __syncthreads();
       return false;
     }
-    const int* expA = reinterpret_cast<const int*>(sm + buf * kDfBufBytes + 2 * kDfSlices * kBf16PanelBytes);
-    const int* expB = expA + tc::kRows;
     // the slice products into four accumulators, by one thread
     if (tid == 0) {
       tc::fenceAfterSync();
@@ -1599,9 +1610,9 @@ static __device__ __noinline__ bool tcDfTrailingStep(df64* M, int Tn, int J, lon
         for (int sj = 0; si + sj < kDfSlices; ++sj) {
           const int o = min(si + sj, 3);
           const uint32_t d = tmem + (uint32_t)(o * tc::kRows);
-          const uint32_t aAddr = bufAddr[buf] + (uint32_t)si * kBf16PanelBytes;
-          const uint32_t bAddr = bufAddr[buf] + (uint32_t)(kDfSlices + sj) * kBf16PanelBytes;
-          for (int sK = 0; sK < kTile / 16; ++sK) {
+          const uint32_t aAddr = opAddr + (uint32_t)si * kDfPanelBytes;
+          const uint32_t bAddr = opAddr + (uint32_t)(kDfSlices + sj) * kDfPanelBytes;
+          for (int sK = 0; sK < kDfK / 16; ++sK) {
             const uint32_t off = (uint32_t)sK * 4096u;
             tc::mmaBf16(d, tc::smemDesc(aAddr + off), tc::smemDesc(bAddr + off), idesc, used[o] || sK > 0);
           }
@@ -1633,11 +1644,14 @@ static __device__ __noinline__ bool tcDfTrailingStep(df64* M, int Tn, int J, lon
     tc::fenceAfterSync();
     if (!__syncthreads_and(ok)) {
       tc::mbarWait(mbarMma, phMma ^ 1u, kTcWaitNs);  // the MMAs in flight, once more
-      tc::mbarWait(mbarLd[buf ^ 1], buf ? phLd0 : phLd1, kTcWaitNs);
       __syncthreads();
       return false;
     }
+    // the operand buffer is free: the next super-block's copies overlap this C update
+    if (tid == 0 && sb + stride < nsb) issueLoads(sbGeo(sb + stride, J, Tn), eb ^ 1);
     {
+      const int* expA = reinterpret_cast<const int*>(sm + kDfOpBytes + (uint32_t)eb * kDfExpBytes);
+      const int* expB = expA + tc::kRows;
       const int eR = expA[R];
       const uint32_t lanes = (uint32_t)(32 * q) << 16;
 #pragma unroll
@@ -1667,7 +1681,71 @@ static __device__ __noinline__ bool tcDfTrailingStep(df64* M, int Tn, int J, lon
       }
     }
     tc::fenceBeforeSync();
-    __syncthreads();  // TMEM read and this buffer consumed before the next super-block
+    __syncthreads();  // TMEM read and this exponent buffer consumed before the next super-block
+  }
+  return true;
+}
+
+// Whole-GPU double-float LDL' over pairs of tile columns (J0, J1 = J0 + 1), three grid barriers
+// per pair:
+//  (A0) the off-diagonal tiles of column J0, one warp each; CTA 0's warp 0 takes L_J1,J0, then
+//       updates the diagonal tile (J1, J1) with it and factors it;
+//  (A1) column J1's tiles I > J1, one warp each: the update by column J0 (tile routine),
+//       L_I,J1, and the BF16 slices of the row pair (sliceRowPair);
+//  (B)  the trailing update of both columns at once (tcDfTrailingStep, CTAs 1..), while CTA 0's
+//       warp 0 updates the diagonal tile (J1 + 1, J1 + 1) with both columns and factors it.
+// Only CTA 0's warp 0 factors diagonal tiles, so the pivot statistics stay in its shared memory.
+template <typename T>
+__device__ __noinline__ bool gridLdltStepsDf(GridCtl* g, int nr, int nx, const DevSettings& st, T* M, PivotStats* ps,
+                                             unsigned char* slices, int Tn, int warp, int gw, int GW, bool cta0,
+                                             TcState& tcs) {
+  if (cta0 && warp == 0) tileFactorDiag<T>(M, 0, nr, nx, st, ps);
+  if (!gridSync(g)) return false;
+  for (int J0 = 0; J0 + 1 < Tn; J0 += 2) {
+    const int J1 = J0 + 1;
+    const T* A0 = M + tileBase(Tn, J0, J0);
+    T* A1 = M + tileBase(Tn, J1, J1);
+    // (A0)
+    if (cta0 && warp == 0) {
+      T* L10 = M + tileBase(Tn, J1, J0);
+      tileOffDiag<T>(L10, A0);
+      __syncwarp();
+      tileSyrk<T>(A1, L10, L10, A0);
+      __syncwarp();
+      tileFactorDiag<T>(A1, J1, nr, nx, st, ps);
+    } else {
+      for (int I = J1 + 1 + (gw - 1); I < Tn; I += GW - 1) tileOffDiag<T>(M + tileBase(Tn, I, J0), A0);
+    }
+    if (!gridSync(g)) return false;
+    // (A1)
+    for (int I = J1 + 1 + gw; I < Tn; I += GW) {
+      T* C = M + tileBase(Tn, I, J1);
+      tileSyrk<T>(C, M + tileBase(Tn, I, J0), M + tileBase(Tn, J1, J0), A0);
+      __syncwarp();
+      tileOffDiag<T>(C, A1);
+      sliceRowPair(M, Tn, I, J0, slices);
+    }
+    if (!gridSync(g)) return false;
+    if (J1 + 1 >= Tn) break;
+    // (B)
+    const int rem = Tn - J1 - 1;
+    const int nb = (rem + 3) >> 2;
+    const long long nsb = (long long)nb * (nb + 1) / 2;
+    if (cta0) {
+      if (warp == 0) {
+        T* An = M + tileBase(Tn, J1 + 1, J1 + 1);
+        tileSyrk<T>(An, M + tileBase(Tn, J1 + 1, J0), M + tileBase(Tn, J1 + 1, J0), A0);
+        __syncwarp();
+        tileSyrk<T>(An, M + tileBase(Tn, J1 + 1, J1), M + tileBase(Tn, J1 + 1, J1), A1);
+        __syncwarp();
+        tileFactorDiag<T>(An, J1 + 1, nr, nx, st, ps);
+      }
+    } else if (!tcDfTrailingStep(M, Tn, J1, nsb, slices, tcs.stage, tcs.tmem, tcs.mbar, tcs.mbar + 8u, tcs.phMma,
+                                 tcs.phLd0)) {
+      if (threadIdx.x == 0) atomicExch(&g->error, 1);
+      return false;
+    }
+    if (!gridSync(g)) return false;
   }
   return true;
 }
@@ -1679,14 +1757,8 @@ static __device__ __noinline__ bool tcDfTrailingStep(df64* M, int Tn, int J, lon
 //      tile routine and factors it (one-column lookahead); barrier.
 // Every root entry receives its updates in increasing J with the same operations and rounding as
 // the single-CTA factor, so both give the same bits. Only warp 0 of CTA 0 factors diagonal tiles,
-// so the pivot statistics stay in CTA 0's shared memory (ps). `stage` holds gridStageBytes.
-// tensor-core state of a CTA for the length of one factorisation job
-struct TcState {
-  unsigned char* stage;  // kGridTcStageBytes, 128-byte aligned
-  uint32_t tmem, mbar;   // TMEM base; three mbarriers at mbar, mbar + 8, mbar + 16
-  uint32_t phMma, phLd0, phLd1;
-};
-
+// so the pivot statistics stay in CTA 0's shared memory (ps). `stage` holds gridStageBytes. The
+// double-float factor runs over column pairs instead (gridLdltStepsDf).
 template <typename T>
 __device__ __noinline__ bool gridLdltSteps(GridCtl* g, int nr, int nx, const DevSettings& st, T* M, PivotStats* ps,
                                            T* stage, unsigned char* slices, int Tn, int warp, int gw, int GW, bool cta0,
@@ -1719,7 +1791,11 @@ __device__ __noinline__ bool gridLdlt(GridCtl* g, int nr, int nx, const DevSetti
     tc::fenceAfterSync();
     tcs.tmem = sTmem;
   }
-  const bool ok = gridLdltSteps<T>(g, nr, nx, st, M, ps, stage, slices, Tn, warp, gw, GW, cta0, tcs);
+  bool ok;
+  if constexpr (ArithOf<T>::v == 2)
+    ok = gridLdltStepsDf<T>(g, nr, nx, st, M, ps, slices, Tn, warp, gw, GW, cta0, tcs);
+  else
+    ok = gridLdltSteps<T>(g, nr, nx, st, M, ps, stage, slices, Tn, warp, gw, GW, cta0, tcs);
   if (kTc && !cta0) {
     tc::fenceBeforeSync();
     __syncthreads();
@@ -1738,11 +1814,7 @@ __device__ __noinline__ bool gridLdltSteps(GridCtl* g, int nr, int nx, const Dev
   if (!gridSync(g)) return false;
   for (int J = 0; J + 1 < Tn; ++J) {
     T* Ajj = M + tileBase(Tn, J, J);
-    for (int I = J + 1 + gw; I < Tn; I += GW) {
-      tileOffDiag<T>(M + tileBase(Tn, I, J), Ajj);
-      // double-float: the warp that finished L_IJ writes its BF16 slices for the trailing update
-      if constexpr (ArithOf<T>::v == 2) sliceTile(M, Tn, I, J, slices);
-    }
+    for (int I = J + 1 + gw; I < Tn; I += GW) tileOffDiag<T>(M + tileBase(Tn, I, J), Ajj);
     if (!gridSync(g)) return false;
     const int rem = Tn - J - 1;
     const int nb = (rem + 3) >> 2;
@@ -1763,12 +1835,6 @@ __device__ __noinline__ bool gridLdltSteps(GridCtl* g, int nr, int nx, const Dev
     if constexpr (sizeof(T) == 4) {
       if (!tcTrailingStep(M, Tn, J, nsb, tcs.stage, tcs.tmem, tcs.mbar, tcs.mbar + 8u, tcs.mbar + 16u, tcs.phMma,
                           tcs.phLd0, tcs.phLd1)) {
-        if (threadIdx.x == 0) atomicExch(&g->error, 1);
-        return false;
-      }
-    } else if constexpr (ArithOf<T>::v == 2) {
-      if (!tcDfTrailingStep(M, Tn, J, nsb, slices, tcs.stage, tcs.tmem, tcs.mbar, tcs.mbar + 8u, tcs.mbar + 16u,
-                            tcs.phMma, tcs.phLd0, tcs.phLd1)) {
         if (threadIdx.x == 0) atomicExch(&g->error, 1);
         return false;
       }

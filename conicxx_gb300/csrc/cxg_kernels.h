@@ -49,13 +49,13 @@ inline int64_t krylovDoubles(int nMax, int mMax) {
   return (2 * kGmresDim + 1) * ld + (kGmresDim + 1) * kGmresDim + 4 * kGmresDim + 2;
 }
 
-// Whole-GPU double-float factor: the BF16 slices of each tile column's panels (A = L_IJ and
-// B = L_IJ D_J, six slices each, for every root row) and their row exponents, written once per
-// tile column and copied into shared memory per super-block. Bytes for a root of nr rows
-// (a multiple of 16).
+// Whole-GPU double-float factor: the BF16 slices of each pair of tile columns' panels (A = L_IJ
+// and B = L_IJ D_J over 64 columns, six slices each, for every root row) and their row exponents,
+// written once per column pair and copied into shared memory per super-block. Bytes for a root
+// of nr rows (a multiple of 16).
 inline int64_t dfSliceBytes(int nr) {
   const int64_t rows = (int64_t)((nr + 31) / 32) * 32;
-  return rows * (2 * 6 * 4 * 16) + 2 * rows * 4;
+  return rows * (2 * 6 * 8 * 16) + 2 * rows * 4;
 }
 
 struct LaunchArgs {
