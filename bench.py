@@ -384,7 +384,21 @@ def run_gb300(args, rank, world, local_rank):
             # DRAM bytes of the launch set scale with the number of instances
             traffic = tj["dram_bytes_per_step"] * count / tj["instances"]
             fp64_pipe = tj.get("fp64_pipe_active_frac")
+        # ---- per-timestep contact-pattern change: a new set-up of 1% and 10% of the instances
+        # (cxg_batch_replace: only those planned again, the rest moved on the device) against
+        # setting the whole batch up ----
+        PB = BatchSolver(qps, settings=default_settings(precision=1, warm_start=1))
+        rng_pu = np.random.default_rng(7)
+        pattern_update = {"full_setup_s": setup_s, "workload": "contact instances replaced by new contact instances "
+                          "(other sizes and patterns), the rest kept with values and warm starts"}
+        for pct in (1, 10):
+            k = max(1, count * pct // 100)
+            idx = rng_pu.choice(count, k, replace=False)
+            new = [generators.contact_qp(10_000_000 + 1000 * pct + j) for j in range(k)]
+            pattern_update[f"replace_{pct}pct"] = {"instances": int(k), "s": PB.replace(idx, new)}
+        del PB
         result = dict(
+            pattern_update=pattern_update,
             e2e={"value": count / e2e_s, "unit": "solves/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
             plain_gpu={"value": plain_rate, "unit": "solves/s", "instances": plain_n, "precision": "fp64",
                        "batched_over_plain": (count / (ms * 1e-3)) / plain_rate},

@@ -41,6 +41,7 @@ SIGNATURES = {
     "cxg_batch_sizes": (C.c_int, [vp, i64p, i64p, i64p, i64p]),
     "cxg_batch_offsets": (C.c_int, [vp, C.c_int, i64p, i64p, i64p, i64p]),
     "cxg_batch_update_values": (C.c_int, [vp, dp, dp, dp, dp]),
+    "cxg_batch_replace": (C.c_int, [vp, C.c_int, ip, PP]),
     "cxg_batch_solve": (C.c_int, [vp, dp, dp, dp, IP]),
     "cxg_batch_update_values_device": (C.c_int, [vp, vp, vp, vp, vp, vp]),
     "cxg_batch_solve_device": (C.c_int, [vp, vp, vp, vp, IP, vp]),

@@ -15,6 +15,7 @@
 #include <mutex>
 #include <stdexcept>
 #include <thread>
+#include <type_traits>
 #include <numeric>
 #include <string>
 #include <vector>
@@ -125,6 +126,8 @@ struct cxg_batch {
   cxg_settings st{};      // current settings
   cxg_settings kktSt{};   // KKT fields frozen at setup (kkt_system.cpp:26-31)
   Pools pools;
+  std::vector<Pools> inst;                        // each instance's own plan (offsets from 0), for cxg_batch_replace
+  size_t ipoolCap = 0, dpoolCap = 0;              // device capacity of dIpool / dDpool (entries)
   std::vector<std::vector<int>> Pp, Pi, Ap, Ai;  // patterns for updateData checks
   std::vector<int> order;
   std::vector<Group> groups;
@@ -157,6 +160,7 @@ struct cxg_batch {
   int device = 0;
   bool gridMode = false;                    // one instance, root spread over every SM (launchIpmGrid)
   bool bwdDropped = false;                  // differentiable asked for, not kept (whole-GPU root > 8192 rows)
+  bool bwdStale = false;                    // instances replaced since the last solve: no saved states
   void* dGridCtl = nullptr;                 // its control block
   double* dTrace = nullptr;                 // record_timings: iteration traces (count x traceRows rows)
   int traceRows = 0;
@@ -461,6 +465,8 @@ static int uploadPlan(cxg_batch* B) {
   if ((rc = devAlloc(&B->dDesc, N))) return rc;
   if ((rc = devAlloc(&B->dIpool, B->pools.ipool.size()))) return rc;
   if ((rc = devAlloc(&B->dDpool, B->pools.dpool.size()))) return rc;
+  B->ipoolCap = std::max<size_t>(B->pools.ipool.size(), 1);
+  B->dpoolCap = std::max<size_t>(B->pools.dpool.size(), 1);
   if ((rc = devAlloc(&B->dPx, (size_t)B->pools.totPx))) return rc;
   if ((rc = devAlloc(&B->dq, (size_t)B->pools.totQ))) return rc;
   if ((rc = devAlloc(&B->dAx, (size_t)B->pools.totAx))) return rc;
@@ -494,10 +500,71 @@ static int uploadPlan(cxg_batch* B) {
   return CXG_OK;
 }
 
+// Plans problems[j] into dst[slots[j]], j < k, each into its own pool (offsets from 0), on
+// worker threads over contiguous chunks. Throws LimitError / std::exception as planInstance does.
+static void planInstances(const cxg_problem* problems, const int* slots, int k, const cxg_settings& st,
+                          std::vector<Pools>& dst) {
+  const int hw = (int)std::max(1u, std::thread::hardware_concurrency());
+  const int nth = std::max(1, std::min({hw, 32, k / 16}));
+  std::vector<std::string> fail((size_t)nth);
+  std::vector<char> failLimit((size_t)nth, 0);
+  auto work = [&](int t) {
+    const int lo = (int)((int64_t)k * t / nth), hi = (int)((int64_t)k * (t + 1) / nth);
+    try {
+      for (int j = lo; j < hi; ++j) {
+        Pools one;
+        planInstance(problems[j], st, one);
+        dst[(size_t)slots[j]] = std::move(one);
+      }
+    } catch (const LimitError& ex) {
+      fail[(size_t)t] = ex.what();
+      failLimit[(size_t)t] = 1;
+    } catch (const std::exception& ex) {
+      fail[(size_t)t] = ex.what();
+    }
+  };
+  if (nth == 1) {
+    work(0);
+  } else {
+    std::vector<std::thread> pool;
+    pool.reserve((size_t)nth);
+    for (int t = 0; t < nth; ++t) pool.emplace_back(work, t);
+    for (std::thread& th : pool) th.join();
+  }
+  for (int t = 0; t < nth; ++t)
+    if (!fail[(size_t)t].empty()) {
+      if (failLimit[(size_t)t]) throw LimitError(fail[(size_t)t]);
+      throw std::runtime_error(fail[(size_t)t]);
+    }
+}
+
+// The checks of cxg_batch_create on instance i of a batch of `count` (CXG_OK, or the error code
+// with the message set).
+static int checkBatchProblem(const cxg_problem& pr, int i, int count, const cxg_settings& st);
+
 static std::string checkFinite(const double* v, int64_t n, const char* name) {
   for (int64_t i = 0; i < n; ++i)
     if (!std::isfinite(v[i])) return std::string(name) + " contains a non-finite value";
   return "";
+}
+
+static int checkBatchProblem(const cxg_problem& pr, int i, int count, const cxg_settings& st) {
+  std::string e = validateProblem(pr);
+  if (!e.empty()) return setErr(CXG_E_INVALID, "instance " + std::to_string(i) + ": " + e);
+  e = checkPlanCounts(pr);
+  if (!e.empty()) return setErr(CXG_E_UNSUPPORTED, "instance " + std::to_string(i) + ": " + e);
+  e = checkFinite(pr.Px, pr.Pp[pr.n], "P");
+  if (e.empty()) e = checkFinite(pr.Ax, pr.Ap[pr.n], "A");
+  if (e.empty()) e = checkFinite(pr.q, pr.n, "q");
+  if (e.empty()) e = checkFinite(pr.b, pr.m, "b");
+  if (!e.empty()) return setErr(CXG_E_INVALID, "instance " + std::to_string(i) + ": " + e);
+  const int nr = pr.n + pr.zero_dim;
+  if (nr > kCtaMaxRoot && !(count == 1 && st.whole_gpu_root >= 0 && nr <= kGridMaxRoot))
+    return setErr(CXG_E_UNSUPPORTED,
+                  "instance " + std::to_string(i) + ": n + zero_dim = " + std::to_string(nr) +
+                      " exceeds the one-CTA root (4096 rows); a single instance (count 1, whole_gpu_root >= 0) "
+                      "takes the whole-GPU root up to " + std::to_string(kGridMaxRoot) + " rows");
+  return CXG_OK;
 }
 
 extern "C" int cxg_batch_create(cxg_batch** out, int count, const cxg_problem* problems,
@@ -512,24 +579,8 @@ extern "C" int cxg_batch_create(cxg_batch** out, int count, const cxg_problem* p
     cxg_default_settings(&st);
     st.precision = CXG_PRECISION_MIXED;
   }
-  for (int i = 0; i < count; ++i) {
-    std::string e = validateProblem(problems[i]);
-    if (!e.empty()) return setErr(CXG_E_INVALID, "instance " + std::to_string(i) + ": " + e);
-    e = checkPlanCounts(problems[i]);
-    if (!e.empty()) return setErr(CXG_E_UNSUPPORTED, "instance " + std::to_string(i) + ": " + e);
-    const cxg_problem& pr = problems[i];
-    e = checkFinite(pr.Px, pr.Pp[pr.n], "P");
-    if (e.empty()) e = checkFinite(pr.Ax, pr.Ap[pr.n], "A");
-    if (e.empty()) e = checkFinite(pr.q, pr.n, "q");
-    if (e.empty()) e = checkFinite(pr.b, pr.m, "b");
-    if (!e.empty()) return setErr(CXG_E_INVALID, "instance " + std::to_string(i) + ": " + e);
-    const int nr = pr.n + pr.zero_dim;
-    if (nr > kCtaMaxRoot && !(count == 1 && st.whole_gpu_root >= 0 && nr <= kGridMaxRoot))
-      return setErr(CXG_E_UNSUPPORTED,
-                    "instance " + std::to_string(i) + ": n + zero_dim = " + std::to_string(nr) +
-                        " exceeds the one-CTA root (4096 rows); a single instance (count 1, whole_gpu_root >= 0) "
-                        "takes the whole-GPU root up to " + std::to_string(kGridMaxRoot) + " rows");
-  }
+  for (int i = 0; i < count; ++i)
+    if (int rc = checkBatchProblem(problems[i], i, count, st)) return rc;
   // One instance whose root one CTA cannot hold, or when asked: spread the root over every SM.
   // (cxg_solver_setup asks for it from kGridAutoRoot rows on.)
   const int nr0 = problems[0].n + problems[0].zero_dim;
@@ -548,36 +599,11 @@ extern "C" int cxg_batch_create(cxg_batch** out, int count, const cxg_problem* p
   try {
     // Host planning, the set-up cost when contact patterns change: contiguous chunks of instances
     // are planned on worker threads into their own pools, then appended in instance order.
-    const int hw = (int)std::max(1u, std::thread::hardware_concurrency());
-    const int nth = std::max(1, std::min({hw, 32, count / 16}));
-    std::vector<Pools> part((size_t)nth);
-    std::vector<std::string> fail((size_t)nth);
-    std::vector<char> failLimit((size_t)nth, 0);
-    auto work = [&](int t) {
-      const int lo = (int)((int64_t)count * t / nth), hi = (int)((int64_t)count * (t + 1) / nth);
-      try {
-        for (int i = lo; i < hi; ++i) planInstance(problems[i], st, part[(size_t)t]);
-      } catch (const LimitError& ex) {
-        fail[(size_t)t] = ex.what();
-        failLimit[(size_t)t] = 1;
-      } catch (const std::exception& ex) {
-        fail[(size_t)t] = ex.what();
-      }
-    };
-    if (nth == 1) {
-      work(0);
-    } else {
-      std::vector<std::thread> pool;
-      pool.reserve((size_t)nth);
-      for (int t = 0; t < nth; ++t) pool.emplace_back(work, t);
-      for (std::thread& th : pool) th.join();
-    }
-    for (int t = 0; t < nth; ++t)
-      if (!fail[(size_t)t].empty()) {
-        if (failLimit[(size_t)t]) throw LimitError(fail[(size_t)t]);
-        throw std::runtime_error(fail[(size_t)t]);
-      }
-    for (const Pools& pp : part) appendPools(B->pools, pp);
+    B->inst.resize((size_t)count);
+    std::vector<int> all((size_t)count);
+    std::iota(all.begin(), all.end(), 0);
+    planInstances(problems, all.data(), count, st, B->inst);
+    for (const Pools& pp : B->inst) appendPools(B->pools, pp);
     for (int i = 0; i < count; ++i) {
       const cxg_problem& pr = problems[i];
       B->Pp.emplace_back(pr.Pp, pr.Pp + pr.n + 1);
@@ -632,6 +658,232 @@ extern "C" int cxg_batch_create(cxg_batch** out, int count, const cxg_problem* p
   B->hRes.resize((size_t)count);
   B->setupTime = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
   *out = B;
+  return CXG_OK;
+}
+
+// ------------------------------------------------------------------------------------------
+// replacing instances (new patterns) without a new batch
+// ------------------------------------------------------------------------------------------
+// Per-instance arrays of a batch, in the concatenated layouts: values (P, q, A, b), solutions and
+// warm starts. moveKernel copies each kept instance's segments from the old layout to the new one
+// (one CTA per instance).
+struct MoveArgs {
+  static constexpr int kArrays = 10;
+  const double* src[kArrays];
+  double* dst[kArrays];
+  int kind[kArrays];          // 0: P values, 1: n-vector, 2: A values, 3: m-vector
+  const int64_t* oldOff;      // count x 4: vPx, vQ, vAx, vB of the old layout
+  const int64_t* newOff;      // count x 4, new layout
+  const int64_t* len;         // count x 4: nnzP, n, nnzA, m
+  const unsigned char* keep;  // count
+};
+
+__global__ void __launch_bounds__(256) moveKernel(MoveArgs a, int count) {
+  const int i = blockIdx.x;
+  if (i >= count || !a.keep[i]) return;
+  for (int k = 0; k < MoveArgs::kArrays; ++k) {
+    if (!a.src[k]) continue;
+    const int kd = a.kind[k];
+    const int64_t so = a.oldOff[4 * i + kd], dof = a.newOff[4 * i + kd], ln = a.len[4 * i + kd];
+    for (int64_t t = threadIdx.x; t < ln; t += blockDim.x) a.dst[k][dof + t] = a.src[k][so + t];
+  }
+}
+
+extern "C" int cxg_batch_replace(cxg_batch* B, int k, const int* indices, const cxg_problem* problems) {
+  if (!B) return setErr(CXG_E_INVALID, "null batch");
+  if (k < 0 || (k > 0 && (!indices || !problems))) return setErr(CXG_E_INVALID, "null indices or problems");
+  if (k == 0) return CXG_OK;
+  if (B->gridMode) return setErr(CXG_E_UNSUPPORTED, "a whole-GPU single instance is set up anew with cxg_solver_setup");
+  std::vector<char> seen((size_t)B->count, 0);
+  for (int j = 0; j < k; ++j) {
+    const int i = indices[j];
+    if (i < 0 || i >= B->count) return setErr(CXG_E_INVALID, "instance index out of range");
+    if (seen[(size_t)i]) return setErr(CXG_E_INVALID, "instance index repeated");
+    seen[(size_t)i] = 1;
+    if (int rc = checkBatchProblem(problems[j], i, B->count, B->kktSt)) return rc;
+  }
+  const auto t0 = std::chrono::steady_clock::now();
+  CX_CUDA(cudaSetDevice(B->device));
+  CX_CUDA(cudaStreamSynchronize(B->stream));
+  // (1) host plans of the new instances, then the concatenated pools in instance order
+  std::vector<Pools> fresh((size_t)B->count);
+  try {
+    planInstances(problems, indices, k, B->kktSt, fresh);
+  } catch (const LimitError& ex) {
+    return setErr(CXG_E_UNSUPPORTED, std::string("planning refused: ") + ex.what());
+  } catch (const std::exception& ex) {
+    return setErr(CXG_E_NOMEM, std::string("planning failed: ") + ex.what());
+  }
+  const std::vector<InstanceDesc> oldDesc = B->pools.desc;
+  // The new plans go after the pool's end (the replaced instances' old blocks stay as unused
+  // space, so only the tail is uploaded); when unused space would exceed the live plans, the
+  // pool is rebuilt from the per-instance plans.
+  const size_t oldI = B->pools.ipool.size(), oldD = B->pools.dpool.size();
+  size_t liveI = 0, newI = 0;
+  for (int j = 0; j < k; ++j) newI += fresh[(size_t)indices[j]].ipool.size() + 1;
+  for (const Pools& pp : B->inst) liveI += pp.ipool.size() + 1;
+  for (int j = 0; j < k; ++j) liveI -= B->inst[(size_t)indices[j]].ipool.size() + 1;
+  liveI += newI;
+  const bool compact = oldI + newI > 2 * liveI + (size_t(1) << 20);
+  for (int j = 0; j < k; ++j) {
+    const int i = indices[j];
+    B->inst[(size_t)i] = std::move(fresh[(size_t)i]);
+    const cxg_problem& pr = problems[j];
+    B->Pp[(size_t)i].assign(pr.Pp, pr.Pp + pr.n + 1);
+    B->Pi[(size_t)i].assign(pr.Pi, pr.Pi + pr.Pp[pr.n]);
+    B->Ap[(size_t)i].assign(pr.Ap, pr.Ap + pr.n + 1);
+    B->Ai[(size_t)i].assign(pr.Ai, pr.Ai + pr.Ap[pr.n]);
+    if (!compact) {
+      appendPools(B->pools, B->inst[(size_t)i]);
+      B->pools.desc[(size_t)i] = B->pools.desc.back();
+      B->pools.desc.pop_back();
+    }
+  }
+  if (compact) {
+    Pools np;
+    for (const Pools& pp : B->inst) appendPools(np, pp);
+    B->pools = std::move(np);
+  } else {
+    // the value arrays stay in instance order: offsets from the instances' sizes
+    int64_t oPx = 0, oQ = 0, oAx = 0, oB = 0;
+    for (InstanceDesc& D : B->pools.desc) {
+      D.vPx = oPx; D.vQ = oQ; D.vAx = oAx; D.vB = oB;
+      D.vX = D.vQ; D.vS = D.vB; D.vZ = D.vB;
+      oPx += D.nnzPu; oQ += D.n; oAx += D.nnzA; oB += D.m;
+    }
+    B->pools.totPx = oPx; B->pools.totQ = oQ; B->pools.totAx = oAx; B->pools.totB = oB;
+  }
+  if (B->st.differentiable) {
+    int64_t off = 0;
+    for (InstanceDesc& D : B->pools.desc) {
+      D.bwdOff = off;
+      off += bwdLayout(D.nr, D.n, D.m, D.nsoc).total;
+    }
+    B->bwdTotal = off;
+  }
+  // (2) the per-instance device arrays in the new layout: kept instances' values, solutions and
+  //     warm starts moved on the device, the new instances' values uploaded, their warm starts off
+  const size_t N = (size_t)B->count;
+  std::vector<int64_t> oldOff(4 * N), newOff(4 * N), len(4 * N);
+  std::vector<unsigned char> keep(N, 1);
+  for (int j = 0; j < k; ++j) keep[(size_t)indices[j]] = 0;
+  for (size_t i = 0; i < N; ++i) {
+    const InstanceDesc &O = oldDesc[i], &D = B->pools.desc[i];
+    oldOff[4 * i] = O.vPx; oldOff[4 * i + 1] = O.vQ; oldOff[4 * i + 2] = O.vAx; oldOff[4 * i + 3] = O.vB;
+    newOff[4 * i] = D.vPx; newOff[4 * i + 1] = D.vQ; newOff[4 * i + 2] = D.vAx; newOff[4 * i + 3] = D.vB;
+    len[4 * i] = D.nnzPu; len[4 * i + 1] = D.n; len[4 * i + 2] = D.nnzA; len[4 * i + 3] = D.m;
+  }
+  double* na[MoveArgs::kArrays] = {};
+  double** olds[MoveArgs::kArrays] = {&B->dPx, &B->dq, &B->dAx, &B->db, &B->dx, &B->ds, &B->dz, &B->dWx, &B->dWs, &B->dWz};
+  const int kinds[MoveArgs::kArrays] = {0, 1, 2, 3, 1, 3, 3, 1, 3, 3};
+  const int64_t totals[4] = {B->pools.totPx, B->pools.totQ, B->pools.totAx, B->pools.totB};
+  int64_t* dOld = nullptr;
+  int64_t* dNew = nullptr;
+  int64_t* dLen = nullptr;
+  unsigned char* dKeep = nullptr;
+  int rc = CXG_OK;
+  auto cleanup = [&]() {
+    for (double* p : na) if (p) cudaFree(p);
+    if (dOld) cudaFree(dOld);
+    if (dNew) cudaFree(dNew);
+    if (dLen) cudaFree(dLen);
+    if (dKeep) cudaFree(dKeep);
+  };
+  for (int a = 0; a < MoveArgs::kArrays && !rc; ++a) rc = devAlloc(&na[a], (size_t)std::max<int64_t>(totals[kinds[a]], 1));
+  if (!rc) rc = devAlloc(&dOld, 4 * N);
+  if (!rc) rc = devAlloc(&dNew, 4 * N);
+  if (!rc) rc = devAlloc(&dLen, 4 * N);
+  if (!rc) rc = devAlloc(&dKeep, N);
+  if (rc) { cleanup(); return rc; }
+  cudaError_t ce = cudaMemcpy(dOld, oldOff.data(), 4 * N * sizeof(int64_t), cudaMemcpyHostToDevice);
+  if (ce == cudaSuccess) ce = cudaMemcpy(dNew, newOff.data(), 4 * N * sizeof(int64_t), cudaMemcpyHostToDevice);
+  if (ce == cudaSuccess) ce = cudaMemcpy(dLen, len.data(), 4 * N * sizeof(int64_t), cudaMemcpyHostToDevice);
+  if (ce == cudaSuccess) ce = cudaMemcpy(dKeep, keep.data(), N, cudaMemcpyHostToDevice);
+  // the new instances' values at their new offsets, their solutions and warm starts zero
+  for (int a = 0; a < MoveArgs::kArrays && ce == cudaSuccess; ++a)
+    if (a >= 4) ce = cudaMemset(na[a], 0, (size_t)std::max<int64_t>(totals[kinds[a]], 1) * sizeof(double));
+  for (int j = 0; j < k && ce == cudaSuccess; ++j) {
+    const cxg_problem& pr = problems[j];
+    const InstanceDesc& D = B->pools.desc[(size_t)indices[j]];
+    if (D.nnzPu) ce = cudaMemcpy(na[0] + D.vPx, pr.Px, (size_t)D.nnzPu * sizeof(double), cudaMemcpyHostToDevice);
+    if (ce == cudaSuccess && D.n) ce = cudaMemcpy(na[1] + D.vQ, pr.q, (size_t)D.n * sizeof(double), cudaMemcpyHostToDevice);
+    if (ce == cudaSuccess && D.nnzA) ce = cudaMemcpy(na[2] + D.vAx, pr.Ax, (size_t)D.nnzA * sizeof(double), cudaMemcpyHostToDevice);
+    if (ce == cudaSuccess && D.m) ce = cudaMemcpy(na[3] + D.vB, pr.b, (size_t)D.m * sizeof(double), cudaMemcpyHostToDevice);
+    if (ce == cudaSuccess) ce = cudaMemset(B->dHaveWarm + indices[j], 0, 1);
+  }
+  if (ce == cudaSuccess) {
+    MoveArgs ma{};
+    for (int a = 0; a < MoveArgs::kArrays; ++a) {
+      ma.src[a] = *olds[a];
+      ma.dst[a] = na[a];
+      ma.kind[a] = kinds[a];
+    }
+    ma.oldOff = dOld;
+    ma.newOff = dNew;
+    ma.len = dLen;
+    ma.keep = dKeep;
+    moveKernel<<<B->count, 256>>>(ma, B->count);
+    ce = cudaGetLastError();
+    if (ce == cudaSuccess) ce = cudaDeviceSynchronize();
+  }
+  if (ce != cudaSuccess) {
+    cleanup();
+    return setErr(CXG_E_CUDA, std::string("replace: ") + cudaGetErrorString(ce));
+  }
+  for (int a = 0; a < MoveArgs::kArrays; ++a) {
+    cudaFree(*olds[a]);
+    *olds[a] = na[a];
+    na[a] = nullptr;
+  }
+  cleanup();
+  // (3) the plan arrays, the size buckets (grids, scratch, counters) and the saved adjoint states
+  if (B->dCounters) cudaFree(B->dCounters);
+  B->dCounters = nullptr;
+  if ((rc = buildGroups(B))) return rc;
+  if ((rc = devAlloc(&B->dCounters, B->groups.size() + 1))) return rc;
+  // pool arrays: the new tail only, unless they were rebuilt or outgrew the capacity
+  auto syncPool = [&](auto*& dptr, size_t& cap, const auto& host, size_t oldSize) -> int {
+    using E = typename std::decay<decltype(host[0])>::type;
+    const size_t nsz = host.size();
+    size_t from = compact ? 0 : oldSize;
+    if (nsz > cap) {
+      const size_t ncap = nsz + nsz / 2;
+      E* np_ = nullptr;
+      if (int r = devAlloc(&np_, ncap)) return r;
+      if (!compact && oldSize) {
+        const cudaError_t e2 = cudaMemcpy(np_, dptr, oldSize * sizeof(E), cudaMemcpyDeviceToDevice);
+        if (e2 != cudaSuccess) { cudaFree(np_); return setErr(CXG_E_CUDA, cudaGetErrorString(e2)); }
+      }
+      cudaFree(dptr);
+      dptr = np_;
+      cap = ncap;
+    }
+    if (nsz > from) {
+      const cudaError_t e2 = cudaMemcpy(dptr + from, host.data() + from, (nsz - from) * sizeof(E), cudaMemcpyHostToDevice);
+      if (e2 != cudaSuccess) return setErr(CXG_E_CUDA, cudaGetErrorString(e2));
+    }
+    return CXG_OK;
+  };
+  if ((rc = syncPool(B->dIpool, B->ipoolCap, B->pools.ipool, oldI))) return rc;
+  if ((rc = syncPool(B->dDpool, B->dpoolCap, B->pools.dpool, oldD))) return rc;
+  CX_CUDA(cudaMemcpy(B->dDesc, B->pools.desc.data(), N * sizeof(InstanceDesc), cudaMemcpyHostToDevice));
+  CX_CUDA(cudaMemcpy(B->dOrder, B->order.data(), N * sizeof(int), cudaMemcpyHostToDevice));
+  if (B->st.differentiable) {
+    double* g[6] = {B->dBwd, B->dGx, B->dGq, B->dGb, B->dGP, B->dGA};
+    for (double* p : g)
+      if (p) cudaFree(p);
+    B->dBwd = B->dGx = B->dGq = B->dGb = B->dGP = B->dGA = nullptr;
+    if ((rc = devAlloc(&B->dBwd, (size_t)std::max<int64_t>(B->bwdTotal, 1))) ||
+        (rc = devAlloc(&B->dGx, (size_t)std::max<int64_t>(B->pools.totQ, 1))) ||
+        (rc = devAlloc(&B->dGq, (size_t)std::max<int64_t>(B->pools.totQ, 1))) ||
+        (rc = devAlloc(&B->dGb, (size_t)std::max<int64_t>(B->pools.totB, 1))) ||
+        (rc = devAlloc(&B->dGP, (size_t)std::max<int64_t>(B->pools.totPx, 1))) ||
+        (rc = devAlloc(&B->dGA, (size_t)std::max<int64_t>(B->pools.totAx, 1))))
+      return rc;
+    B->bwdStale = true;
+  }
+  B->graphValid = false;
+  B->setupTime = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
   return CXG_OK;
 }
 
@@ -866,6 +1118,7 @@ static int enqueueSolve(cxg_batch* B, cudaStream_t s) {
 // Device-side solve through the captured graph (re-captured when the settings change).
 static int runSolve(cxg_batch* B, cudaStream_t s) {
   if (int rc = ensureTrace(B)) return rc;
+  B->bwdStale = false;
   // the whole-GPU form is one cooperative launch: enqueued directly, not through a graph
   if (B->gridMode) return enqueueSolve(B, s);
   const DevSettings ds = makeDevSettings(B->st, B->kktSt);
@@ -1293,6 +1546,7 @@ static int checkDifferentiable(cxg_batch* B) {
     return setErr(CXG_E_UNSUPPORTED, "backward is offered up to 8192 root rows on the whole-GPU root");
   if (!B->dBwd) return setErr(CXG_E_NOT_SETUP, "backward needs settings.differentiable = 1 at set-up");
   if (B->forkJoin.empty()) return setErr(CXG_E_NOT_SETUP, "backward before any solve");
+  if (B->bwdStale) return setErr(CXG_E_NOT_SETUP, "backward after cxg_batch_replace needs a solve first");
   return CXG_OK;
 }
 
@@ -1357,6 +1611,7 @@ extern "C" int cxg_batch_solve_device_noalloc(cxg_batch* B, double* x, double* s
                                               void* stream) {
   if (!B) return setErr(CXG_E_INVALID, "null batch");
   if (B->gridMode) return setErr(CXG_E_UNSUPPORTED, "the whole-GPU root of a single large instance has its own scratch");
+  B->bwdStale = false;
   int dev = -1;
   CX_CUDA(cudaGetDevice(&dev));
   if (dev != B->device) return setErr(CXG_E_INVALID, "the batch lives on another device: make that device current");

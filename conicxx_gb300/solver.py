@@ -175,9 +175,11 @@ class BatchSolver:
         self._h = h
         self.qps = list(qps)
         self.count = len(qps)
-        a, b, c_, d = C.c_int64(), C.c_int64(), C.c_int64(), C.c_int64()
-        check(lib().cxg_batch_sizes(h, C.byref(a), C.byref(b), C.byref(c_), C.byref(d)), "cxg_batch_sizes")
-        self.nnzP, self.n_total, self.nnzA, self.m_total = a.value, b.value, c_.value, d.value
+        self._keep = None  # the library copied everything
+        self._offsets()
+
+    def _offsets(self):
+        qps = self.qps
         self.n_off = np.zeros(self.count + 1, np.int64)
         self.m_off = np.zeros(self.count + 1, np.int64)
         self.p_off = np.zeros(self.count + 1, np.int64)
@@ -187,7 +189,33 @@ class BatchSolver:
             self.m_off[i + 1] = self.m_off[i] + qp.m
             self.p_off[i + 1] = self.p_off[i] + qp.P.nnz
             self.a_off[i + 1] = self.a_off[i] + qp.A.nnz
-        self._keep = None  # the library copied everything
+        self.nnzP, self.n_total, self.nnzA, self.m_total = (int(self.p_off[-1]), int(self.n_off[-1]),
+                                                            int(self.a_off[-1]), int(self.m_off[-1]))
+
+    def replace(self, indices, qps):
+        """A new set-up of instances indices[j] as qps[j] (new patterns and sizes allowed), the
+        others kept with their values and warm starts (cxg_batch_replace). Returns the seconds the
+        call took (host planning of the replaced instances, device re-layout)."""
+        import time
+
+        indices = [int(i) for i in indices]
+        structs, keep = [], []
+        for qp in qps:
+            s_, k_ = make_problem_struct(qp)
+            structs.append(s_)
+            keep.append(k_)
+        arr = (_abi.Problem * max(1, len(qps)))(*structs)
+        idx = np.ascontiguousarray(indices, dtype=np.int32)
+        t0 = time.perf_counter()
+        check(lib().cxg_batch_replace(self._h, len(indices), iptr(idx), arr), "cxg_batch_replace")
+        dt = time.perf_counter() - t0
+        for i, qp in zip(indices, qps):
+            self.qps[i] = qp
+        self._offsets()
+        a, b, c_, d = C.c_int64(), C.c_int64(), C.c_int64(), C.c_int64()
+        check(lib().cxg_batch_sizes(self._h, C.byref(a), C.byref(b), C.byref(c_), C.byref(d)), "cxg_batch_sizes")
+        assert (a.value, b.value, c_.value, d.value) == (self.nnzP, self.n_total, self.nnzA, self.m_total)
+        return dt
 
     def __del__(self):
         h = getattr(self, "_h", None)

@@ -210,6 +210,17 @@ int cxg_batch_create(cxg_batch** out, int count, const cxg_problem* problems,
                      const cxg_settings* settings);
 void cxg_batch_destroy(cxg_batch* batch);
 int cxg_batch_count(const cxg_batch* batch);
+/* A new set-up of some instances of a batch (conicxx::Solver::setup of each,
+ * include/conicxx/solver.h:33-56, src/conicxx/solver_impl.cpp:9-55): instance indices[j] becomes
+ * problems[j], j < k, new sparsity patterns and sizes allowed (the per-timestep contact-pattern
+ * change). Only the replaced instances are planned again (symbolic analysis and equilibration of
+ * each, on host threads); the others keep their plans, their values as last set and their
+ * device-resident warm starts, which move to the new layout on the device. The replaced
+ * instances start cold. Offsets (cxg_batch_offsets) and sizes (cxg_batch_sizes) change; with
+ * settings.differentiable, backward needs a solve first. Refused for the whole-GPU single
+ * instance (CXG_E_UNSUPPORTED); errors as cxg_batch_create, the batch unchanged on a validation
+ * error. Synchronises the device. */
+int cxg_batch_replace(cxg_batch* batch, int k, const int* indices, const cxg_problem* problems);
 /* Sizes of the concatenated value/solution arrays: sum of nnz(P upper), n, nnz(A), m. */
 int cxg_batch_sizes(const cxg_batch* batch, int64_t* nnzP, int64_t* n_total, int64_t* nnzA,
                     int64_t* m_total);
