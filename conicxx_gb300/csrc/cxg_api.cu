@@ -128,6 +128,7 @@ struct cxg_batch {
   Pools pools;
   std::vector<Pools> inst;                        // each instance's own plan (offsets from 0), for cxg_batch_replace
   size_t ipoolCap = 0, dpoolCap = 0;              // device capacity of dIpool / dDpool (entries)
+  std::vector<int> edges;                         // size-bucket upper edges on nr (empty: kBucketEdges)
   std::vector<std::vector<int>> Pp, Pi, Ap, Ai;  // patterns for updateData checks
   std::vector<int> order;
   std::vector<Group> groups;
@@ -333,9 +334,11 @@ static int buildGroups(cxg_batch* B) {
   // order: by bucket (descending nr), then by cost descending
   std::vector<int> idx((size_t)N);
   std::iota(idx.begin(), idx.end(), 0);
+  const std::vector<int> edges =
+      B->edges.empty() ? std::vector<int>(std::begin(kBucketEdges), std::end(kBucketEdges)) : B->edges;
   auto bucketOf = [&](int nr) {
     int b = 0;
-    for (int e : kBucketEdges) {
+    for (int e : edges) {
       if (nr <= e) return b;
       ++b;
     }
@@ -456,6 +459,19 @@ static int buildGroups(cxg_batch* B) {
   int rc = devAlloc(&B->dScratch, (size_t)std::max<int64_t>(scratchTotal, 2));
   if (rc) return rc;
   B->scratchCapacity = std::max<int64_t>(scratchTotal, 2);
+  return CXG_OK;
+}
+
+// After buildGroups on a batch already on the device: the per-bucket queue counters, the
+// instance descriptors (their scratch offsets) and the queue order; the captured graph is stale.
+static int refreshGroupsOnDevice(cxg_batch* B) {
+  const size_t N = (size_t)B->count;
+  if (B->dCounters) cudaFree(B->dCounters);
+  B->dCounters = nullptr;
+  if (int rc = devAlloc(&B->dCounters, B->groups.size() + 1)) return rc;
+  CX_CUDA(cudaMemcpy(B->dDesc, B->pools.desc.data(), N * sizeof(InstanceDesc), cudaMemcpyHostToDevice));
+  CX_CUDA(cudaMemcpy(B->dOrder, B->order.data(), N * sizeof(int), cudaMemcpyHostToDevice));
+  B->graphValid = false;
   return CXG_OK;
 }
 
@@ -837,10 +853,8 @@ extern "C" int cxg_batch_replace(cxg_batch* B, int k, const int* indices, const 
   }
   cleanup();
   // (3) the plan arrays, the size buckets (grids, scratch, counters) and the saved adjoint states
-  if (B->dCounters) cudaFree(B->dCounters);
-  B->dCounters = nullptr;
   if ((rc = buildGroups(B))) return rc;
-  if ((rc = devAlloc(&B->dCounters, B->groups.size() + 1))) return rc;
+  if ((rc = refreshGroupsOnDevice(B))) return rc;
   // pool arrays: the new tail only, unless they were rebuilt or outgrew the capacity
   auto syncPool = [&](auto*& dptr, size_t& cap, const auto& host, size_t oldSize) -> int {
     using E = typename std::decay<decltype(host[0])>::type;
@@ -866,8 +880,6 @@ extern "C" int cxg_batch_replace(cxg_batch* B, int k, const int* indices, const 
   };
   if ((rc = syncPool(B->dIpool, B->ipoolCap, B->pools.ipool, oldI))) return rc;
   if ((rc = syncPool(B->dDpool, B->dpoolCap, B->pools.dpool, oldD))) return rc;
-  CX_CUDA(cudaMemcpy(B->dDesc, B->pools.desc.data(), N * sizeof(InstanceDesc), cudaMemcpyHostToDevice));
-  CX_CUDA(cudaMemcpy(B->dOrder, B->order.data(), N * sizeof(int), cudaMemcpyHostToDevice));
   if (B->st.differentiable) {
     double* g[6] = {B->dBwd, B->dGx, B->dGq, B->dGb, B->dGP, B->dGA};
     for (double* p : g)
@@ -1254,16 +1266,8 @@ extern "C" int cxg_batch_describe(const cxg_batch* B, char* buf, int buflen) {
 }
 
 // ------------------------------------------------------------------------------------------
-// autotuner: threads per instance for each size bucket, by timing the bucket's launch alone
+// autotuner: size-bucket edges, then threads per instance for each bucket, by timing whole solves
 // ------------------------------------------------------------------------------------------
-// Resident CTAs of one bucket for a block size (the persistent grid).
-static int bucketGrid(const Group& g, int block, int numSM) {
-  int occ = 0;
-  const cudaError_t oe = ipmOccupancy(&occ, block, g.smem, g.fp32);
-  if (oe != cudaSuccess || occ < 1) occ = 1;
-  return std::max(1, std::min(g.count, occ * numSM));
-}
-
 // Lays the per-bucket scratch regions out again after grids changed; reallocates if it grew.
 static int relayoutScratch(cxg_batch* B) {
   int64_t total = 0;
@@ -1295,44 +1299,105 @@ extern "C" int cxg_batch_autotune(cxg_batch* B, int trials, char* report, int re
   tst.warm_start = 0;  // trials leave the warm-start state alone
   tst.record_timings = 0;
   const DevSettings ds = makeDevSettings(tst, B->kktSt);
-  static const int kCand[] = {32, 64, 128, 256};
   std::string rep;
+  // (1) the size-bucket edges: each candidate set is planned (buckets, SM shares, scratch) and a
+  //     whole concurrent solve timed; the fastest set is kept
+  {
+    static const std::vector<std::vector<int>> kEdgeSets = {
+        {32, 64, 96, 128, 192, 256, 384, 512, 1024, 2048, 4096},
+        {64, 128, 192, 256, 384, 512, 1024, 2048, 4096},
+        {16, 32, 48, 64, 96, 128, 160, 192, 256, 384, 512, 1024, 2048, 4096},
+        {32, 64, 128, 192, 256, 384, 512, 1024, 2048, 4096},
+        {48, 96, 144, 192, 256, 384, 512, 1024, 2048, 4096}};
+    const cxg_settings saved = B->st;
+    B->st = tst;
+    cudaEvent_t a0 = nullptr, a1 = nullptr;
+    CX_CUDA(cudaEventCreate(&a0));
+    CX_CUDA(cudaEventCreate(&a1));
+    int best = -1, rc0 = CXG_OK;
+    float bestMs = 0.0f;
+    char line[160];
+    for (size_t e = 0; e < kEdgeSets.size() && rc0 == CXG_OK; ++e) {
+      B->edges = kEdgeSets[e];
+      if ((rc0 = buildGroups(B)) || (rc0 = refreshGroupsOnDevice(B))) break;
+      std::vector<float> ms;
+      for (int t = 0; t < trials + 1 && rc0 == CXG_OK; ++t) {
+        cudaError_t ce = cudaEventRecord(a0, B->stream);
+        if (ce == cudaSuccess && (rc0 = runSolve(B, B->stream))) break;
+        if (ce == cudaSuccess) ce = cudaEventRecord(a1, B->stream);
+        if (ce == cudaSuccess) ce = cudaEventSynchronize(a1);
+        float v = 0.0f;
+        if (ce == cudaSuccess) ce = cudaEventElapsedTime(&v, a0, a1);
+        if (ce != cudaSuccess) rc0 = setErr(CXG_E_CUDA, std::string("autotune: ") + cudaGetErrorString(ce));
+        if (t > 0) ms.push_back(v);  // the first solve of each set captures its graph
+      }
+      if (rc0) break;
+      std::sort(ms.begin(), ms.end());
+      const float med = ms[ms.size() / 2];
+      std::snprintf(line, sizeof(line), "edges set %d (%d size groups): %.3f ms\n", (int)e, (int)B->groups.size(), med);
+      rep += line;
+      if (best < 0 || med < bestMs) {
+        best = (int)e;
+        bestMs = med;
+      }
+    }
+    cudaEventDestroy(a0);
+    cudaEventDestroy(a1);
+    B->st = saved;
+    if (rc0) return rc0;
+    B->edges = kEdgeSets[(size_t)best];
+    int rcb = buildGroups(B);
+    if (!rcb) rcb = refreshGroupsOnDevice(B);
+    if (rcb) return rcb;
+    std::snprintf(line, sizeof(line), "-> edges set %d\n", best);
+    rep += line;
+  }
+  // (2) threads per instance for each size bucket, one bucket at a time, by timing the whole
+  //     concurrent solve (the buckets share the SMs, so a shape that is faster alone can lengthen
+  //     the others' time): for each candidate the SM shares and scratch are laid out again
+  static const int kCand[] = {32, 64, 128, 256};
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   CX_CUDA(cudaEventCreate(&e0));
   CX_CUDA(cudaEventCreate(&e1));
+  const cxg_settings saved = B->st;
+  B->st = tst;
   int rc = CXG_OK;
+  auto timeSolve = [&](float& med) -> int {
+    partitionGrids(B, numSM);
+    if (int r = relayoutScratch(B)) return r;
+    B->graphValid = false;
+    std::vector<float> ms;
+    for (int t = 0; t < trials + 1; ++t) {
+      cudaError_t ce = cudaEventRecord(e0, B->stream);
+      if (ce == cudaSuccess)
+        if (int r = runSolve(B, B->stream)) return r;
+      if (ce == cudaSuccess) ce = cudaEventRecord(e1, B->stream);
+      if (ce == cudaSuccess) ce = cudaEventSynchronize(e1);
+      float v = 0.0f;
+      if (ce == cudaSuccess) ce = cudaEventElapsedTime(&v, e0, e1);
+      if (ce != cudaSuccess) return setErr(CXG_E_CUDA, std::string("autotune: ") + cudaGetErrorString(ce));
+      if (t > 0) ms.push_back(v);  // the first solve of each shape captures its graph
+    }
+    std::sort(ms.begin(), ms.end());
+    med = ms[ms.size() / 2];
+    return CXG_OK;
+  };
   for (size_t gi = 0; gi < B->groups.size() && rc == CXG_OK; ++gi) {
     Group& g = B->groups[gi];
-    // one trial scratch buffer large enough for the largest candidate grid of this bucket
-    int64_t need = 2;
-    for (int b : kCand)
-      if (b >= 64 || g.lay.nrMax <= 64) need = std::max<int64_t>(need, g.stride * bucketGrid(g, b, numSM));
-    double* trialScratch = nullptr;
-    if ((rc = devAlloc(&trialScratch, (size_t)need))) break;
-    int bestBlock = g.block;
+    const int start = g.block;
+    int bestBlock = start;
     float bestMs = 0.0f;
     char line[256];
     std::snprintf(line, sizeof(line), "bucket nr<=%d (%d instances):", g.lay.nrMax, g.count);
     rep += line;
     for (int b : kCand) {
       if (b < 64 && g.lay.nrMax > 64) continue;  // one warp only for small roots
-      const int grid = bucketGrid(g, b, numSM);
-      std::vector<float> ms;
-      for (int t = 0; t < trials + 1 && rc == CXG_OK; ++t) {
-        cudaError_t ce = cudaMemsetAsync(B->dCounters + g.counterIdx, 0, sizeof(int), B->stream);
-        if (ce == cudaSuccess) ce = cudaEventRecord(e0, B->stream);
-        const LaunchArgs a = solveArgs(B, g, ds, B->dCounters + g.counterIdx, trialScratch);
-        if (ce == cudaSuccess) ce = launchIpm(a, grid, b, g.smem, g.fp32, B->stream);
-        if (ce == cudaSuccess) ce = cudaEventRecord(e1, B->stream);
-        if (ce == cudaSuccess) ce = cudaEventSynchronize(e1);
-        float v = 0.0f;
-        if (ce == cudaSuccess) ce = cudaEventElapsedTime(&v, e0, e1);
-        if (ce != cudaSuccess) rc = setErr(CXG_E_CUDA, std::string("autotune: ") + cudaGetErrorString(ce));
-        if (t > 0) ms.push_back(v);  // the first run of each shape is a warm-up
-      }
-      if (rc) break;
-      std::sort(ms.begin(), ms.end());
-      const float med = ms[ms.size() / 2];
+      int occ = 0;
+      if (ipmOccupancy(&occ, b, g.smem, g.fp32) != cudaSuccess || occ < 1) occ = 1;
+      g.block = b;
+      g.occupancy = occ;
+      float med = 0.0f;
+      if ((rc = timeSolve(med))) break;
       std::snprintf(line, sizeof(line), " %d threads %.3f ms;", b, med);
       rep += line;
       if (bestMs == 0.0f || med < bestMs) {
@@ -1340,7 +1405,6 @@ extern "C" int cxg_batch_autotune(cxg_batch* B, int trials, char* report, int re
         bestBlock = b;
       }
     }
-    cudaFree(trialScratch);
     if (rc) break;
     g.block = bestBlock;
     {
@@ -1353,6 +1417,7 @@ extern "C" int cxg_batch_autotune(cxg_batch* B, int trials, char* report, int re
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
+  B->st = saved;
   if (rc) return rc;
   partitionGrids(B, numSM);
   if ((rc = relayoutScratch(B))) return rc;

@@ -271,13 +271,14 @@ int cxg_batch_backward_device(cxg_batch* batch, const double* dL_dx, double* dq,
 #define CXG_NOALLOC_SCRATCH_BYTES (32ll << 20)
 int cxg_batch_solve_device_noalloc(cxg_batch* batch, double* x, double* s, double* z, cxg_info* info,
                                    void* stream);
-/* Autotuner (no reference counterpart): for every size bucket, times the bucket's persistent
- * IPM launch alone with 32 (roots of at most 64 rows), 64, 128 and 256 threads per instance (trials timed runs after one
- * warm-up each, median kept) and keeps the fastest for later solves; grids follow from the
- * occupancy of the chosen shape and the per-CTA working memory is laid out again. The trials
+/* Autotuner (no reference counterpart), by timing whole concurrent solves of the batch (trials
+ * timed solves after one warm-up each, median kept): (1) the size-bucket edges on the root size,
+ * from five candidate sets (finer and coarser than the built-in one), each planned with its SM
+ * shares and working memory; (2) then, one bucket at a time, 32 (roots of at most 64 rows), 64,
+ * 128 or 256 threads per instance. The fastest choices are kept for later solves. The trials
  * solve the current values with warm start off and overwrite the last solution (solve again to
- * read one). Allocates temporary device memory. report (may be NULL) receives one line per
- * bucket with the measured times. */
+ * read one). Allocates device memory. report (may be NULL) receives one line per edge set and
+ * one line per bucket with the measured times. */
 int cxg_batch_autotune(cxg_batch* batch, int trials, char* report, int reportLen);
 /* Kernel launches enqueued by the last solve/backward call of this batch. */
 int cxg_batch_last_launches(const cxg_batch* batch);
