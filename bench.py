@@ -657,8 +657,9 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=1024)
     ap.add_argument("--plain-instances", type=int, default=16)
     ap.add_argument("--count", type=int, default=COUNT, help="contact instances per GPU")
-    ap.add_argument("--autotune", action="store_true",
-                    help="pick threads per instance for each size bucket by timing (cxg_batch_autotune) before timing")
+    ap.add_argument("--no-autotune", dest="autotune", action="store_false",
+                    help="skip cxg_batch_autotune (size-bucket edges and threads per bucket picked by timing whole "
+                         "solves before the timed steps; on by default)")
     ap.add_argument("--entry", default="graph", choices=["graph", "noalloc"],
                     help="graph: the captured concurrent-bucket solve (default); noalloc: the allocation-free "
                          "entry point (direct launches, buckets in sequence)")
@@ -715,6 +716,7 @@ def main():
             "scaling": "weak", "vs_baseline": None, "dtype": "mixed fp32-factor/fp64",
             "data": "synthetic (seeded contact generator)",
             "config": {"workload": workload(args.count), "count_per_gpu": args.count, "entry": args.entry,
+                       "autotuned": bool(args.autotune),
                        "parallelism": f"instances x{world}",
                        "l2": "flushed between timed steps (256 MB device write outside the step events)",
                        "solved_fraction": solved_frac, "statuses": statuses, "warm_start": False},
