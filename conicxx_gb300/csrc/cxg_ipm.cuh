@@ -1551,17 +1551,18 @@ static __device__ __noinline__ void sliceRowPair(const df64* M, int Tn, int I, i
 }
 
 // The trailing update of column pair (J - 1, J) over the super-blocks this CTA owns (sb =
-// blockIdx.x - 1, + gridDim.x - 1, ...; tile rows and columns from J + 1). Pipeline: a
-// super-block's slices and exponents arrive by bulk copies (TMA); its 84 MMAs run; meanwhile its
-// 64 C entries per thread are loaded into registers; once the MMAs are complete the next
-// super-block's copies are issued (the operand buffer is free; the exponents alternate between
-// two buffers) and overlap this super-block's C update. Shared memory `sm` (128-byte aligned):
-// kDfStageBytes. `tmem`: this CTA's 512 accumulator columns; mbarriers: MMA completion and
-// copies, with their phase parities. Returns false when a wait ran out (after waiting once more
-// for the copies and MMAs in flight).
+// blockIdx.x - 1, + gridDim.x - 1, ...; tile rows and columns from J + 1). Per super-block: its
+// slices and exponents arrive by bulk copies (TMA); one thread issues its 84 MMAs; once they are
+// complete the operand buffer holds the super-block's C tiles instead (bulk copies from HBM),
+// which are updated there from the accumulators and written back by bulk copies; once those have
+// read the buffer, the next super-block's slices are issued into it (the exponents alternate
+// between two buffers). Shared memory `sm` (128-byte aligned): kDfStageBytes. `tmem`: this CTA's
+// 512 accumulator columns; mbarriers: MMA completion, slice copies and C copies, with their phase
+// parities. Returns false when a wait ran out (after waiting once more for what is in flight).
 static __device__ __noinline__ bool tcDfTrailingStep(df64* M, int Tn, int J, long long nsb, const unsigned char* slices,
                                                      unsigned char* sm, uint32_t tmem, uint32_t mbarMma,
-                                                     uint32_t mbarLd, uint32_t& phMma, uint32_t& phLd) {
+                                                     uint32_t mbarLd, uint32_t mbarC, uint32_t& phMma, uint32_t& phLd,
+                                                     uint32_t& phC) {
   const int tid = threadIdx.x;
   const long long first = (long long)blockIdx.x - 1, stride = (long long)gridDim.x - 1;
   if (first >= nsb) return true;
@@ -1569,9 +1570,11 @@ static __device__ __noinline__ bool tcDfTrailingStep(df64* M, int Tn, int J, lon
   const uint32_t opAddr = tc::smemAddr(sm);
   const uint32_t expAddr[2] = {opAddr + kDfOpBytes, opAddr + kDfOpBytes + kDfExpBytes};
   constexpr int kPlanes = kDfSlices * (kDfK / 8);  // per operand
+  constexpr uint32_t kTileBytesDf = (uint32_t)kTileElems * 8u;
+  df64* Cs = reinterpret_cast<df64*>(sm);  // the C tiles, where the operands were
   // thread 0: the slices of super-block g's A rows (tiles I0 ..) and B rows (K0 ..), exponents
   // into exponent buffer eb
-  auto issueLoads = [&](const SbGeo& g, int eb) {
+  auto issueOps = [&](const SbGeo& g, int eb) {
     const int nt[2] = {g.ni, g.nk};
     const int64_t row0[2] = {(int64_t)g.I0 * kTile, (int64_t)g.K0 * kTile};
     uint32_t bytes = 0;
@@ -1587,9 +1590,20 @@ static __device__ __noinline__ bool tcDfTrailingStep(df64* M, int Tn, int J, lon
                    (uint32_t)nt[o] * 128u, mbarLd);
     }
   };
+  // thread 0: super-block g's C tiles (tile t = 4 a + b at t x 8448 bytes) into the operand buffer
+  auto issueC = [&](const SbGeo& g) {
+    uint32_t bytes = 0;
+    for (int t = 0; t < 16; ++t)
+      if (sbTile(g, t)) bytes += kTileBytesDf;
+    tc::mbarArriveExpectTx(mbarC, bytes);
+    for (int t = 0; t < 16; ++t)
+      if (sbTile(g, t))
+        tc::bulkLoad(opAddr + (uint32_t)t * kTileBytesDf, M + tileBase(Tn, g.I0 + (t >> 2), g.K0 + (t & 3)),
+                     kTileBytesDf, mbarC);
+  };
   if (tid == 0) {
-    tc::fenceProxyAsyncGlobal();  // the slices written this step (generic stores) before the copies
-    issueLoads(sbGeo(first, J, Tn), 0);
+    tc::fenceProxyAsyncGlobal();  // the slices and C written this step (generic stores) before the copies
+    issueOps(sbGeo(first, J, Tn), 0);
   }
   int eb = 0;
   for (long long sb = first; sb < nsb; sb += stride, eb ^= 1) {
@@ -1619,50 +1633,39 @@ static __device__ __noinline__ bool tcDfTrailingStep(df64* M, int Tn, int J, lon
           used[o] = true;
         }
       tc::commitTo(mbarMma);
-    }
-    // C -= scaled sum of the accumulators: warp w owns TMEM lanes 32 (w % 4) .. +31 (its rows) and
-    // columns 64 (w / 4) .. +63. All 64 of a thread's C entries are loaded before the MMAs are
-    // waited for (their latency overlaps the products), then updated eight columns at a time.
-    const int warp = tid >> 5, lane = tid & 31;
-    const int q = warp & 3, hh = (warp >> 2) & 1;
-    const int R = 32 * q + lane;
-    const bool rowOk = (R >> 5) < g.ni;
-    // the two C tiles of this thread's columns in row R's tile row (tile columns K0 + 2 hh, + 1)
-    const int64_t colBase0 = tileBase(Tn, g.I0 + (R >> 5), g.K0 + 2 * hh) + (R & 31);
-    const int64_t colBase1 = tileBase(Tn, g.I0 + (R >> 5), g.K0 + 2 * hh + 1) + (R & 31);
-    auto cIdx = [&](int jj) -> int64_t { return ((jj >> 5) ? colBase1 : colBase0) + (jj & 31) * kTileLd; };
-    float ch[64], cl[64];
-#pragma unroll
-    for (int j = 0; j < 64; ++j) {
-      const bool upd = rowOk && sbTile(g, 4 * (R >> 5) + 2 * hh + (j >> 5));
-      const df64 v = upd ? M[cIdx(j)] : df64(0.0f, 0.0f);
-      ch[j] = v.hi;
-      cl[j] = v.lo;
+      // the C tiles into the operand buffer once the MMAs have read it
+      const bool okM = tc::mbarWait(mbarMma, phMma, kTcWaitNs);
+      if (okM) issueC(g);
     }
     const bool ok = tc::mbarWait(mbarMma, phMma, kTcWaitNs);
     phMma ^= 1u;
+    const bool okC = ok && tc::mbarWait(mbarC, phC, kTcWaitNs);
+    if (ok) phC ^= 1u;
     tc::fenceAfterSync();
-    if (!__syncthreads_and(ok)) {
-      tc::mbarWait(mbarMma, phMma ^ 1u, kTcWaitNs);  // the MMAs in flight, once more
+    if (!__syncthreads_and(ok && okC)) {
+      tc::mbarWait(mbarMma, phMma ^ 1u, kTcWaitNs);  // the MMAs and copies in flight, once more
+      if (ok) tc::mbarWait(mbarC, phC ^ 1u, kTcWaitNs);
       __syncthreads();
       return false;
     }
-    // the operand buffer is free: the next super-block's copies overlap this C update
-    if (tid == 0 && sb + stride < nsb) issueLoads(sbGeo(sb + stride, J, Tn), eb ^ 1);
+    // C -= scaled sum of the accumulators, in shared memory: warp w owns TMEM lanes 32 (w % 4) ..
+    // +31 (its rows) and columns 64 (w / 4) .. +63, eight at a time
     {
+      const int warp = tid >> 5, lane = tid & 31;
+      const int q = warp & 3, hh = (warp >> 2) & 1;
+      const int R = 32 * q + lane;
       const int* expA = reinterpret_cast<const int*>(sm + kDfOpBytes + (uint32_t)eb * kDfExpBytes);
       const int* expB = expA + tc::kRows;
       const int eR = expA[R];
       const uint32_t lanes = (uint32_t)(32 * q) << 16;
-#pragma unroll
+#pragma unroll 2
       for (int cb = 0; cb < 8; ++cb) {
         const int c0 = 64 * hh + 8 * cb;
         float d[4][8];
         tc::tmemLoad8x4(tmem + lanes + (uint32_t)c0, (uint32_t)tc::kRows, d);
-        // branch-free over the eight entries (independent chains); only the stores are predicated
 #pragma unroll
         for (int j = 0; j < 8; ++j) {
-          const int Cc = c0 + j, jj = 8 * cb + j;
+          const int Cc = c0 + j;
           float h, e1, h2, e2;
           dfTwoSum(d[0][j], d[1][j], h, e1);
           dfTwoSum(h, d[2][j], h2, e2);
@@ -1675,14 +1678,32 @@ static __device__ __noinline__ bool tcDfTrailingStep(df64* M, int Tn, int J, lon
           const int ex = eR + expB[Cc];
           const int ex1 = min(max(ex >> 1, -126), 127), ex2 = min(max(ex - (ex >> 1), -126), 127);
           const float f1 = __int_as_float((ex1 + 127) << 23), f2 = __int_as_float((ex2 + 127) << 23);
-          const df64 r = df64(ch[jj], cl[jj]) - df64(__fmul_rn(__fmul_rn(sh, f1), f2), __fmul_rn(__fmul_rn(sl, f1), f2));
-          if (rowOk && sbTile(g, 4 * (R >> 5) + (Cc >> 5))) M[cIdx(jj)] = r;
+          const int t = 4 * (R >> 5) + (Cc >> 5);
+          if (sbTile(g, t)) {
+            df64& cref = Cs[t * kTileElems + (Cc & 31) * kTileLd + (R & 31)];
+            cref = cref - df64(__fmul_rn(__fmul_rn(sh, f1), f2), __fmul_rn(__fmul_rn(sl, f1), f2));
+          }
         }
       }
     }
+    tc::fenceProxyAsyncShared();  // the updated tiles visible to the bulk stores
     tc::fenceBeforeSync();
-    __syncthreads();  // TMEM read and this exponent buffer consumed before the next super-block
+    __syncthreads();  // TMEM read, the C tiles updated, this exponent buffer consumed
+    if (tid == 0) {
+      for (int t = 0; t < 16; ++t)
+        if (sbTile(g, t))
+          tc::bulkStore(M + tileBase(Tn, g.I0 + (t >> 2), g.K0 + (t & 3)), opAddr + (uint32_t)t * kTileBytesDf,
+                        kTileBytesDf);
+      tc::bulkCommit();
+      tc::bulkWaitRead0();  // the stores have read the buffer: the next slices may land in it
+      if (sb + stride < nsb) issueOps(sbGeo(sb + stride, J, Tn), eb ^ 1);
+    }
   }
+  if (tid == 0) {
+    tc::bulkWait0();
+    tc::fenceProxyAsyncGlobal();  // the stores before the grid barrier's generic release
+  }
+  __syncthreads();
   return true;
 }
 
@@ -1740,8 +1761,8 @@ __device__ __noinline__ bool gridLdltStepsDf(GridCtl* g, int nr, int nx, const D
         __syncwarp();
         tileFactorDiag<T>(An, J1 + 1, nr, nx, st, ps);
       }
-    } else if (!tcDfTrailingStep(M, Tn, J1, nsb, slices, tcs.stage, tcs.tmem, tcs.mbar, tcs.mbar + 8u, tcs.phMma,
-                                 tcs.phLd0)) {
+    } else if (!tcDfTrailingStep(M, Tn, J1, nsb, slices, tcs.stage, tcs.tmem, tcs.mbar, tcs.mbar + 8u, tcs.mbar + 16u,
+                                 tcs.phMma, tcs.phLd0, tcs.phLd1)) {
       if (threadIdx.x == 0) atomicExch(&g->error, 1);
       return false;
     }
