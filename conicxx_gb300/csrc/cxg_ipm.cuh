@@ -1965,6 +1965,16 @@ __device__ void ctaBlockBackward(const T* M, int Tn, int b0, int b1, T* y) {
   }
 }
 
+// L2 prefetch of tile rows [I0, I1) of tile column j (contiguous in the packed layout), spread
+// over nt threads: one prefetch per 128-byte line.
+template <typename T>
+__device__ __forceinline__ void prefetchTileRun(const T* M, int Tn, int I0, int I1, int j, int t, int nt) {
+  if (I0 >= I1) return;
+  const char* p = reinterpret_cast<const char*>(M + tileBase(Tn, I0, j));
+  const int64_t bytes = (int64_t)(I1 - I0) * kTileElems * (int64_t)sizeof(T);
+  for (int64_t o = (int64_t)t * 128; o < bytes; o += (int64_t)nt * 128) asm volatile("prefetch.global.L2 [%0];" ::"l"(p + o));
+}
+
 template <typename T>
 __device__ __noinline__ bool gridSolve(GridCtl* g, int nr, const T* M, T* y) {
   const int Tn = rootTiles(nr);
@@ -1977,8 +1987,24 @@ __device__ __noinline__ bool gridSolve(GridCtl* g, int nr, const T* M, T* y) {
   auto scaleBlock = [&](int B) {  // one warp
     for (int j = blo(B); j < bhi(B); ++j) y[j * 32 + lane] /= M[tileBase(Tn, j, j) + lane * kTileLd + lane];
   };
+  // CTA 0's step reads its tiles one dependent round after another; the last CTA, whose warps
+  // have no far tiles to update at this size, prefetches them into L2 one step ahead.
+  const bool pf = (int)blockIdx.x == (int)gridDim.x - 1 && !drv;
+  auto prefetchFwd = [&](int B) {  // the tiles of forward step B: block B+1 from block B, block B+1 itself
+    if (B + 1 >= NB) return;
+    for (int j = blo(B); j < bhi(B); ++j) prefetchTileRun<T>(M, Tn, blo(B + 1), bhi(B + 1), j, threadIdx.x, blockDim.x);
+    for (int j = blo(B + 1); j < bhi(B + 1); ++j) prefetchTileRun<T>(M, Tn, j, bhi(B + 1), j, threadIdx.x, blockDim.x);
+  };
+  auto prefetchBwd = [&](int B) {  // the tiles of backward step B: block B-1 from block B, block B-1 itself
+    if (B < 1) return;
+    for (int k = blo(B - 1); k < bhi(B - 1); ++k) {
+      prefetchTileRun<T>(M, Tn, blo(B), bhi(B), k, threadIdx.x, blockDim.x);
+      prefetchTileRun<T>(M, Tn, k, bhi(B - 1), k, threadIdx.x, blockDim.x);
+    }
+  };
   // forward
   if (drv) ctaBlockForward<T>(M, Tn, blo(0), bhi(0), y);
+  if (pf) prefetchFwd(0);
   if (!gridSync(g)) return false;
   for (int B = 0; B + 1 < NB; ++B) {
     if (drv) {
@@ -1994,6 +2020,7 @@ __device__ __noinline__ bool gridSolve(GridCtl* g, int nr, const T* M, T* y) {
       __syncthreads();
       ctaBlockForward<T>(M, Tn, blo(B + 1), bhi(B + 1), y);
     } else {
+      if (pf) prefetchFwd(B + 1);
       for (int I = blo(B + 2) + ww; I < Tn; I += WW) {
         for (int j = blo(B); j < bhi(B); ++j) {
           warpRowsForward<T>(M + tileBase(Tn, I, j), y + j * 32, y + I * 32);
@@ -2010,6 +2037,7 @@ __device__ __noinline__ bool gridSolve(GridCtl* g, int nr, const T* M, T* y) {
     __syncthreads();
     ctaBlockBackward<T>(M, Tn, blo(NB - 1), bhi(NB - 1), y);
   }
+  if (pf) prefetchBwd(NB - 1);
   if (!gridSync(g)) return false;
   for (int B = NB - 1; B >= 1; --B) {
     if (drv) {
@@ -2023,6 +2051,7 @@ __device__ __noinline__ bool gridSolve(GridCtl* g, int nr, const T* M, T* y) {
       __syncthreads();
       ctaBlockBackward<T>(M, Tn, blo(B - 1), bhi(B - 1), y);
     } else {
+      if (pf) prefetchBwd(B - 1);
       for (int K = blo(B - 1) - 1 - ww; K >= 0; K -= WW) {
         for (int j = bhi(B) - 1; j >= blo(B); --j) {
           warpRowsBackward<T>(M + tileBase(Tn, j, K), y + j * 32, y + K * 32);
