@@ -1707,19 +1707,195 @@ static __device__ __noinline__ bool tcDfTrailingStep(df64* M, int Tn, int J, lon
   return true;
 }
 
-// Whole-GPU double-float LDL' over pairs of tile columns (J0, J1 = J0 + 1), three grid barriers
-// per pair:
+// FP32 trailing update on the tensor cores over a pair of tile columns (J0, J0 + 1): C_IK -=
+// L_I,pair D_pair L_K,pair^T with K = 64, as three TF32 products A_hi B_lo + A_lo B_hi + A_hi B_hi
+// (each FP32 operand x split as hi = tf32(x), lo = tf32(x - hi)) into one FP32 TMEM accumulator:
+// 24 MMAs of 128 x 128 x 8 per super-block, issued by one thread.
+//
+// Panel area (global, `slices`, within dfSliceBytes): for operand o (0 = A = L, 1 = B = L D), part
+// p (0 = hi, 1 = lo) and k-group kg (4 of the 64 columns), the 16 bytes of root row m at
+// ((o * 2 + p) * 16 + kg) * rows * 16 + m * 16: each (o, p, kg) plane is the canonical
+// shared-memory layout of cxg_tc.cuh for every row, so the 128 rows of a super-block are one
+// contiguous copy per plane.
+constexpr int kPairMinTilesF32 = 352;  // 11264 rows
+constexpr int kPairMinTilesDf = 160;   // 5120 rows
+constexpr int kF32Parts = 2;
+constexpr int kF32Groups = kDfK / 4;                                     // 16-byte k-groups per row
+constexpr uint32_t kF32PanelBytes = (uint32_t)tc::kRows * kDfK * 4;      // 32 KB: 128 x 64 TF32
+constexpr uint32_t kF32OpBytes = 2 * kF32Parts * kF32PanelBytes;         // 128 KB of operands
+static_assert(kF32OpBytes >= 16 * kTileBytes, "the C tiles of a super-block must fit in the operand buffer");
+static_assert(kF32OpBytes + 128 <= kGridTcStageBytes, "FP32 pair staging exceeds the stage area");
+static_assert(2 * kF32Parts * kF32Groups * 16 <= 2 * kDfSlices * (kDfK / 8) * 16, "FP32 panels exceed the slice area");
+
+// Writes the TF32 parts (A and B) of the 32 rows of tile row I over the tile columns J0, J0 + 1;
+// one warp, lane rr takes row 32 I + rr. L_I,J0 and L_I,J0+1 must be complete in M.
+static __device__ __noinline__ void sliceRowPair(const float* M, int Tn, int I, int J0, unsigned char* slices) {
+  __syncwarp();
+  const int rr = threadIdx.x & 31;
+  const int64_t rows = (int64_t)Tn * kTile, m = (int64_t)I * kTile + rr;
+  const float* src[2] = {M + tileBase(Tn, I, J0) + rr, M + tileBase(Tn, I, J0 + 1) + rr};
+  const float* dg[2] = {M + tileBase(Tn, J0, J0), M + tileBase(Tn, J0 + 1, J0 + 1)};
+  for (int o = 0; o < 2; ++o) {
+#pragma unroll 2
+    for (int kg = 0; kg < kF32Groups; ++kg) {
+      float hi[4], lo[4];
+#pragma unroll
+      for (int t = 0; t < 4; ++t) {
+        const int k = 4 * kg + t, tt = k >> 5, kk = k & 31;
+        float x = src[tt][kk * kTileLd];
+        if (o) x = x * dg[tt][kk * kTileLd + kk];
+        hi[t] = tc::toTf32(x);
+        lo[t] = tc::toTf32(x - hi[t]);
+      }
+      *reinterpret_cast<float4*>(slices + ((int64_t)(o * kF32Parts) * kF32Groups + kg) * rows * 16 + m * 16) =
+          make_float4(hi[0], hi[1], hi[2], hi[3]);
+      *reinterpret_cast<float4*>(slices + ((int64_t)(o * kF32Parts + 1) * kF32Groups + kg) * rows * 16 + m * 16) =
+          make_float4(lo[0], lo[1], lo[2], lo[3]);
+    }
+  }
+}
+
+// The FP32 trailing update of column pair (J - 1, J), with the sequence of tcDfTrailingStep: per
+// super-block its TF32 parts arrive by bulk copies; one thread issues the 24 MMAs; once they are
+// complete the operand buffer takes the super-block's C tiles (bulk copies), which are updated
+// there from the accumulator and written back by bulk copies; once those have read the buffer,
+// the next super-block's operands are issued into it. Shared memory `sm` (128-byte aligned):
+// kF32OpBytes. `tmem`: this CTA's 128 accumulator columns. Returns false when a wait ran out
+// (after waiting once more for what is in flight).
+static __device__ __noinline__ bool tcF32PairTrailingStep(float* M, int Tn, int J, long long nsb,
+                                                          const unsigned char* slices, unsigned char* sm, uint32_t tmem,
+                                                          uint32_t mbarMma, uint32_t mbarLd, uint32_t mbarC,
+                                                          uint32_t& phMma, uint32_t& phLd, uint32_t& phC) {
+  const int tid = threadIdx.x;
+  const long long first = (long long)blockIdx.x - 1, stride = (long long)gridDim.x - 1;
+  if (first >= nsb) return true;
+  const int64_t rows = (int64_t)Tn * kTile;
+  const uint32_t opAddr = tc::smemAddr(sm);
+  float* Cs = reinterpret_cast<float*>(sm);  // the C tiles, where the operands were
+  // thread 0: the TF32 parts of super-block g's A rows (tiles I0 ..) and B rows (K0 ..)
+  auto issueOps = [&](const SbGeo& g) {
+    const int nt[2] = {g.ni, g.nk};
+    const int64_t row0[2] = {(int64_t)g.I0 * kTile, (int64_t)g.K0 * kTile};
+    uint32_t bytes = 0;
+    for (int o = 0; o < 2; ++o) bytes += (uint32_t)nt[o] * (uint32_t)(kF32Parts * kF32Groups * 512);
+    tc::mbarArriveExpectTx(mbarLd, bytes);
+    for (int o = 0; o < 2; ++o)
+      for (int p = 0; p < kF32Parts; ++p)
+        for (int kg = 0; kg < kF32Groups; ++kg)
+          tc::bulkLoad(opAddr + (uint32_t)(o * kF32Parts + p) * kF32PanelBytes + (uint32_t)kg * 2048u,
+                       slices + ((int64_t)(o * kF32Parts + p) * kF32Groups + kg) * rows * 16 + row0[o] * 16,
+                       (uint32_t)nt[o] * 512u, mbarLd);
+  };
+  // thread 0: super-block g's C tiles (tile t = 4 a + b at t x kTileBytes) into the operand buffer
+  auto issueC = [&](const SbGeo& g) {
+    uint32_t bytes = 0;
+    for (int t = 0; t < 16; ++t)
+      if (sbTile(g, t)) bytes += kTileBytes;
+    tc::mbarArriveExpectTx(mbarC, bytes);
+    for (int t = 0; t < 16; ++t)
+      if (sbTile(g, t))
+        tc::bulkLoad(opAddr + (uint32_t)t * kTileBytes, M + tileBase(Tn, g.I0 + (t >> 2), g.K0 + (t & 3)), kTileBytes,
+                     mbarC);
+  };
+  if (tid == 0) {
+    tc::fenceProxyAsyncGlobal();  // the panels and C written this step (generic stores) before the copies
+    issueOps(sbGeo(first, J, Tn));
+  }
+  for (long long sb = first; sb < nsb; sb += stride) {
+    const SbGeo g = sbGeo(sb, J, Tn);
+    const bool okLd = tc::mbarWait(mbarLd, phLd, kTcWaitNs);
+    phLd ^= 1u;
+    if (!__syncthreads_and(okLd)) {
+      tc::mbarWait(mbarLd, phLd ^ 1u, kTcWaitNs);  // the copies in flight, once more
+      __syncthreads();
+      return false;
+    }
+    if (tid == 0) {
+      tc::fenceAfterSync();
+      constexpr uint32_t idesc = tc::idescTf32(tc::kRows, tc::kRows);
+      const uint32_t aHi = opAddr, aLo = opAddr + kF32PanelBytes, bHi = opAddr + 2 * kF32PanelBytes,
+                     bLo = opAddr + 3 * kF32PanelBytes;
+      for (int sK = 0; sK < kDfK / 8; ++sK) {
+        const uint32_t o = (uint32_t)sK * 4096u;
+        tc::mmaTf32(tmem, tc::smemDesc(aLo + o), tc::smemDesc(bHi + o), idesc, sK > 0);
+        tc::mmaTf32(tmem, tc::smemDesc(aHi + o), tc::smemDesc(bLo + o), idesc, true);
+      }
+      for (int sK = 0; sK < kDfK / 8; ++sK) {
+        const uint32_t o = (uint32_t)sK * 4096u;
+        tc::mmaTf32(tmem, tc::smemDesc(aHi + o), tc::smemDesc(bHi + o), idesc, true);
+      }
+      tc::commitTo(mbarMma);
+      // the C tiles into the operand buffer once the MMAs have read it
+      const bool okM = tc::mbarWait(mbarMma, phMma, kTcWaitNs);
+      if (okM) issueC(g);
+    }
+    const bool ok = tc::mbarWait(mbarMma, phMma, kTcWaitNs);
+    phMma ^= 1u;
+    const bool okC = ok && tc::mbarWait(mbarC, phC, kTcWaitNs);
+    if (ok) phC ^= 1u;
+    tc::fenceAfterSync();
+    if (!__syncthreads_and(ok && okC)) {
+      tc::mbarWait(mbarMma, phMma ^ 1u, kTcWaitNs);  // the MMAs and copies in flight, once more
+      if (ok) tc::mbarWait(mbarC, phC ^ 1u, kTcWaitNs);
+      __syncthreads();
+      return false;
+    }
+    // C -= product, in shared memory: warp w reads TMEM lanes 32 (w % 4) .. +31 (its rows),
+    // columns 64 (w / 4) .. +63, sixteen at a time
+    {
+      const int warp = tid >> 5, lane = tid & 31;
+      if (warp < 8) {
+        const int q = warp & 3, h = warp >> 2;
+        const int R = 32 * q + lane;
+        for (int cb = 0; cb < 4; ++cb) {
+          float d[16];
+          const int c0 = 64 * h + 16 * cb;
+          tc::tmemLoad16(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)c0, d);
+#pragma unroll
+          for (int j = 0; j < 16; ++j) {
+            const int Cc = c0 + j;
+            float& cref = Cs[((R >> 5) * 4 + (Cc >> 5)) * kTileElems + (Cc & 31) * kTileLd + (R & 31)];
+            cref = cref - d[j];
+          }
+        }
+      }
+    }
+    tc::fenceProxyAsyncShared();  // the updated tiles visible to the bulk stores
+    tc::fenceBeforeSync();
+    __syncthreads();  // TMEM read, the C tiles updated
+    if (tid == 0) {
+      for (int t = 0; t < 16; ++t)
+        if (sbTile(g, t))
+          tc::bulkStore(M + tileBase(Tn, g.I0 + (t >> 2), g.K0 + (t & 3)), opAddr + (uint32_t)t * kTileBytes,
+                        kTileBytes);
+      tc::bulkCommit();
+      tc::bulkWaitRead0();  // the stores have read the buffer: the next operands may land in it
+      if (sb + stride < nsb) issueOps(sbGeo(sb + stride, J, Tn));
+    }
+  }
+  if (tid == 0) {
+    tc::bulkWait0();
+    tc::fenceProxyAsyncGlobal();  // the stores before the grid barrier's generic release
+  }
+  __syncthreads();
+  return true;
+}
+
+// Whole-GPU FP32 and double-float LDL' over pairs of tile columns (J0, J1 = J0 + 1), three grid
+// barriers per pair:
 //  (A0) the off-diagonal tiles of column J0, one warp each; CTA 0's warp 0 takes L_J1,J0, then
 //       updates the diagonal tile (J1, J1) with it and factors it;
 //  (A1) column J1's tiles I > J1, one warp each: the update by column J0 (tile routine),
-//       L_I,J1, and the BF16 slices of the row pair (sliceRowPair);
-//  (B)  the trailing update of both columns at once (tcDfTrailingStep, CTAs 1..), while CTA 0's
-//       warp 0 updates the diagonal tile (J1 + 1, J1 + 1) with both columns and factors it.
+//       L_I,J1, and the tensor-core operands of the row pair (sliceRowPair: TF32 parts for FP32,
+//       BF16 slices for double-float);
+//  (B)  the trailing update of both columns at once (tcF32PairTrailingStep / tcDfTrailingStep,
+//       CTAs 1..), while CTA 0's warp 0 updates the diagonal tile (J1 + 1, J1 + 1) with both
+//       columns and factors it.
 // Only CTA 0's warp 0 factors diagonal tiles, so the pivot statistics stay in its shared memory.
 template <typename T>
-__device__ __noinline__ bool gridLdltStepsDf(GridCtl* g, int nr, int nx, const DevSettings& st, T* M, PivotStats* ps,
-                                             unsigned char* slices, int Tn, int warp, int gw, int GW, bool cta0,
-                                             TcState& tcs) {
+__device__ __noinline__ bool gridLdltPairs(GridCtl* g, int nr, int nx, const DevSettings& st, T* M, PivotStats* ps,
+                                           unsigned char* slices, int Tn, int warp, int gw, int GW, bool cta0,
+                                           TcState& tcs) {
   if (cta0 && warp == 0) tileFactorDiag<T>(M, 0, nr, nx, st, ps);
   if (!gridSync(g)) return false;
   for (int J0 = 0; J0 + 1 < Tn; J0 += 2) {
@@ -1761,10 +1937,18 @@ __device__ __noinline__ bool gridLdltStepsDf(GridCtl* g, int nr, int nx, const D
         __syncwarp();
         tileFactorDiag<T>(An, J1 + 1, nr, nx, st, ps);
       }
-    } else if (!tcDfTrailingStep(M, Tn, J1, nsb, slices, tcs.stage, tcs.tmem, tcs.mbar, tcs.mbar + 8u, tcs.mbar + 16u,
-                                 tcs.phMma, tcs.phLd0, tcs.phLd1)) {
-      if (threadIdx.x == 0) atomicExch(&g->error, 1);
-      return false;
+    } else {
+      bool okT;
+      if constexpr (sizeof(T) == 4)
+        okT = tcF32PairTrailingStep(M, Tn, J1, nsb, slices, tcs.stage, tcs.tmem, tcs.mbar, tcs.mbar + 8u,
+                                    tcs.mbar + 16u, tcs.phMma, tcs.phLd0, tcs.phLd1);
+      else
+        okT = tcDfTrailingStep(M, Tn, J1, nsb, slices, tcs.stage, tcs.tmem, tcs.mbar, tcs.mbar + 8u, tcs.mbar + 16u,
+                               tcs.phMma, tcs.phLd0, tcs.phLd1);
+      if (!okT) {
+        if (threadIdx.x == 0) atomicExch(&g->error, 1);
+        return false;
+      }
     }
     if (!gridSync(g)) return false;
   }
@@ -1785,8 +1969,16 @@ __device__ __noinline__ bool gridLdltSteps(GridCtl* g, int nr, int nx, const Dev
                                            T* stage, unsigned char* slices, int Tn, int warp, int gw, int GW, bool cta0,
                                            TcState& tcs);
 
-// `slices`: the double-float factor's panel-slice area (dfSliceBytes(nr), 16-byte aligned);
-// unused by the other arithmetics.
+// Roots of at least this many tile columns factor over column pairs (gridLdltPairs): half the C
+// traffic of the trailing update, but a longer serial chain per pair. Below it, one column at a
+// time (gridLdltSteps: FP32 on the tensor cores, double-float on the CUDA cores).
+template <typename T>
+__device__ __forceinline__ constexpr int pairMinTiles() {
+  return (ArithOf<T>::v == 1) ? kPairMinTilesF32 : kPairMinTilesDf;
+}
+
+// `slices`: the tensor-core panel area of the FP32 and double-float pair forms (dfSliceBytes(nr),
+// 16-byte aligned); unused by FP64.
 template <typename T>
 __device__ __noinline__ bool gridLdlt(GridCtl* g, int nr, int nx, const DevSettings& st, T* M, PivotStats* ps, T* stage,
                                       unsigned char* slices) {
@@ -1812,10 +2004,11 @@ __device__ __noinline__ bool gridLdlt(GridCtl* g, int nr, int nx, const DevSetti
     tc::fenceAfterSync();
     tcs.tmem = sTmem;
   }
-  bool ok;
-  if constexpr (ArithOf<T>::v == 2)
-    ok = gridLdltStepsDf<T>(g, nr, nx, st, M, ps, slices, Tn, warp, gw, GW, cta0, tcs);
-  else
+  bool ok = false;
+  if constexpr (kTc) {
+    if (Tn >= pairMinTiles<T>()) ok = gridLdltPairs<T>(g, nr, nx, st, M, ps, slices, Tn, warp, gw, GW, cta0, tcs);
+  }
+  if (!kTc || Tn < pairMinTiles<T>())
     ok = gridLdltSteps<T>(g, nr, nx, st, M, ps, stage, slices, Tn, warp, gw, GW, cta0, tcs);
   if (kTc && !cta0) {
     tc::fenceBeforeSync();

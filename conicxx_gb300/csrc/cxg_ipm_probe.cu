@@ -136,9 +136,9 @@ static cudaError_t probeGridLaunch(int nr, int nx, const double* K, const double
   if (occ * numSM < 2) return cudaErrorInvalidConfiguration;
   T *M = nullptr, *y = nullptr;
   GridCtl* g = nullptr;
-  unsigned char* slices = nullptr;  // double-float: the panel slices of the tensor-core trailing update
+  unsigned char* slices = nullptr;  // FP32 and double-float: the panels of the tensor-core trailing update
   e = cudaMalloc((void**)&M, (size_t)rootSize(nr) * sizeof(T));
-  if (e == cudaSuccess && ArithOf<T>::v == 2) e = cudaMalloc((void**)&slices, (size_t)dfSliceBytes(nr));
+  if (e == cudaSuccess && ArithOf<T>::v != 0) e = cudaMalloc((void**)&slices, (size_t)dfSliceBytes(nr));
   if (e == cudaSuccess) e = cudaMalloc((void**)&y, (size_t)rootTiles(nr) * kTile * sizeof(T));
   if (e == cudaSuccess) e = cudaMalloc((void**)&g, sizeof(GridCtl));
   if (e == cudaSuccess) e = cudaMemset(g, 0, sizeof(GridCtl));

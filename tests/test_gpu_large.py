@@ -102,6 +102,23 @@ def test_grid_factor_large_root(arith):
     assert recon < {"fp64": 1e-10, "df64": 1e-12, "fp32": 1e-5}[arith]
 
 
+@pytest.mark.parametrize("arith,nr", [("fp32", 12832), ("df64", 5216)])
+def test_grid_factor_pair_form(arith, nr):
+    """Roots above the pair threshold (352 tile columns in FP32, 160 in double-float) factor over
+    column pairs, the trailing update fed by the TF32 parts or BF16 slices written per row pair:
+    the solve against numpy and the residual."""
+    nx = nr - 256
+    K = _quasi_definite(nr, nx, 21)
+    b = np.random.default_rng(22).standard_normal(nr)
+    L, D, x, f = _probe(K, nx, b, arith, -1)
+    assert f[2] == 0 and f[0] == 0 and f[1] == 0
+    xs = np.linalg.solve(K, b)
+    res = np.linalg.norm(K @ x - b) / np.linalg.norm(b)
+    print(arith, nr, "solve", rel(x, xs), "residual", res)
+    assert rel(x, xs) < {"df64": 1e-10, "fp32": 1e-4}[arith]
+    assert res < {"df64": 1e-11, "fp32": 1e-4}[arith]
+
+
 @pytest.mark.parametrize("precision", [_abi.PRECISION_FP64, _abi.PRECISION_MIXED])
 @pytest.mark.parametrize("idx", range(8))
 def test_kats_whole_gpu(kats, idx, precision):
