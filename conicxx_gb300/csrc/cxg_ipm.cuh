@@ -1723,8 +1723,8 @@ constexpr int kF32Parts = 2;
 constexpr int kF32Groups = kDfK / 4;                                     // 16-byte k-groups per row
 constexpr uint32_t kF32PanelBytes = (uint32_t)tc::kRows * kDfK * 4;      // 32 KB: 128 x 64 TF32
 constexpr uint32_t kF32OpBytes = 2 * kF32Parts * kF32PanelBytes;         // 128 KB of operands
-static_assert(kF32OpBytes >= 16 * kTileBytes, "the C tiles of a super-block must fit in the operand buffer");
-static_assert(kF32OpBytes + 128 <= kGridTcStageBytes, "FP32 pair staging exceeds the stage area");
+constexpr int64_t kF32StageBytes = (int64_t)kF32OpBytes + 16 * (int64_t)kTileBytes;  // operands + C tiles
+static_assert(kF32StageBytes + 128 <= kGridTcStageBytes, "FP32 pair staging exceeds the stage area");
 static_assert(2 * kF32Parts * kF32Groups * 16 <= 2 * kDfSlices * (kDfK / 8) * 16, "FP32 panels exceed the slice area");
 
 // Writes the TF32 parts (A and B) of the 32 rows of tile row I over the tile columns J0, J0 + 1;
@@ -1755,13 +1755,15 @@ static __device__ __noinline__ void sliceRowPair(const float* M, int Tn, int I, 
   }
 }
 
-// The FP32 trailing update of column pair (J - 1, J), with the sequence of tcDfTrailingStep: per
-// super-block its TF32 parts arrive by bulk copies; one thread issues the 24 MMAs; once they are
-// complete the operand buffer takes the super-block's C tiles (bulk copies), which are updated
-// there from the accumulator and written back by bulk copies; once those have read the buffer,
-// the next super-block's operands are issued into it. Shared memory `sm` (128-byte aligned):
-// kF32OpBytes. `tmem`: this CTA's 128 accumulator columns. Returns false when a wait ran out
-// (after waiting once more for what is in flight).
+// The FP32 trailing update of column pair (J - 1, J) over the super-blocks this CTA owns (sb =
+// blockIdx.x - 1, + gridDim.x - 1, ...). Shared memory `sm` (128-byte aligned, kF32StageBytes)
+// holds an operand buffer (the TF32 parts, by bulk copies from the panel area) and a C buffer (the
+// super-block's C tiles, by bulk copies from the root). Per super-block: one thread issues the 24
+// MMAs; once they have read the operands, the next super-block's operands are issued into that
+// buffer; the C tiles are updated from the accumulator and written back by bulk stores; once
+// those have read the C buffer, the next super-block's C tiles are issued into it. So the operand
+// copies overlap the epilogue and the C copies the next MMAs. `tmem`: this CTA's 128 accumulator
+// columns. Returns false when a wait ran out (after waiting once more for what is in flight).
 static __device__ __noinline__ bool tcF32PairTrailingStep(float* M, int Tn, int J, long long nsb,
                                                           const unsigned char* slices, unsigned char* sm, uint32_t tmem,
                                                           uint32_t mbarMma, uint32_t mbarLd, uint32_t mbarC,
@@ -1770,8 +1772,8 @@ static __device__ __noinline__ bool tcF32PairTrailingStep(float* M, int Tn, int 
   const long long first = (long long)blockIdx.x - 1, stride = (long long)gridDim.x - 1;
   if (first >= nsb) return true;
   const int64_t rows = (int64_t)Tn * kTile;
-  const uint32_t opAddr = tc::smemAddr(sm);
-  float* Cs = reinterpret_cast<float*>(sm);  // the C tiles, where the operands were
+  const uint32_t opAddr = tc::smemAddr(sm), cAddr = opAddr + kF32OpBytes;
+  float* Cs = reinterpret_cast<float*>(sm + kF32OpBytes);
   // thread 0: the TF32 parts of super-block g's A rows (tiles I0 ..) and B rows (K0 ..)
   auto issueOps = [&](const SbGeo& g) {
     const int nt[2] = {g.ni, g.nk};
@@ -1786,7 +1788,7 @@ static __device__ __noinline__ bool tcF32PairTrailingStep(float* M, int Tn, int 
                        slices + ((int64_t)(o * kF32Parts + p) * kF32Groups + kg) * rows * 16 + row0[o] * 16,
                        (uint32_t)nt[o] * 512u, mbarLd);
   };
-  // thread 0: super-block g's C tiles (tile t = 4 a + b at t x kTileBytes) into the operand buffer
+  // thread 0: super-block g's C tiles (tile t = 4 a + b at t x kTileBytes) into the C buffer
   auto issueC = [&](const SbGeo& g) {
     uint32_t bytes = 0;
     for (int t = 0; t < 16; ++t)
@@ -1794,19 +1796,23 @@ static __device__ __noinline__ bool tcF32PairTrailingStep(float* M, int Tn, int 
     tc::mbarArriveExpectTx(mbarC, bytes);
     for (int t = 0; t < 16; ++t)
       if (sbTile(g, t))
-        tc::bulkLoad(opAddr + (uint32_t)t * kTileBytes, M + tileBase(Tn, g.I0 + (t >> 2), g.K0 + (t & 3)), kTileBytes,
+        tc::bulkLoad(cAddr + (uint32_t)t * kTileBytes, M + tileBase(Tn, g.I0 + (t >> 2), g.K0 + (t & 3)), kTileBytes,
                      mbarC);
   };
   if (tid == 0) {
     tc::fenceProxyAsyncGlobal();  // the panels and C written this step (generic stores) before the copies
-    issueOps(sbGeo(first, J, Tn));
+    const SbGeo g0 = sbGeo(first, J, Tn);
+    issueOps(g0);
+    issueC(g0);
   }
   for (long long sb = first; sb < nsb; sb += stride) {
     const SbGeo g = sbGeo(sb, J, Tn);
+    const bool more = sb + stride < nsb;
     const bool okLd = tc::mbarWait(mbarLd, phLd, kTcWaitNs);
     phLd ^= 1u;
     if (!__syncthreads_and(okLd)) {
       tc::mbarWait(mbarLd, phLd ^ 1u, kTcWaitNs);  // the copies in flight, once more
+      tc::mbarWait(mbarC, phC, kTcWaitNs);
       __syncthreads();
       return false;
     }
@@ -1825,9 +1831,9 @@ static __device__ __noinline__ bool tcF32PairTrailingStep(float* M, int Tn, int 
         tc::mmaTf32(tmem, tc::smemDesc(aHi + o), tc::smemDesc(bHi + o), idesc, true);
       }
       tc::commitTo(mbarMma);
-      // the C tiles into the operand buffer once the MMAs have read it
+      // the next super-block's operands once the MMAs have read this one's
       const bool okM = tc::mbarWait(mbarMma, phMma, kTcWaitNs);
-      if (okM) issueC(g);
+      if (okM && more) issueOps(sbGeo(sb + stride, J, Tn));
     }
     const bool ok = tc::mbarWait(mbarMma, phMma, kTcWaitNs);
     phMma ^= 1u;
@@ -1837,6 +1843,7 @@ static __device__ __noinline__ bool tcF32PairTrailingStep(float* M, int Tn, int 
     if (!__syncthreads_and(ok && okC)) {
       tc::mbarWait(mbarMma, phMma ^ 1u, kTcWaitNs);  // the MMAs and copies in flight, once more
       if (ok) tc::mbarWait(mbarC, phC ^ 1u, kTcWaitNs);
+      if (ok && more) tc::mbarWait(mbarLd, phLd, kTcWaitNs);
       __syncthreads();
       return false;
     }
@@ -1866,11 +1873,11 @@ static __device__ __noinline__ bool tcF32PairTrailingStep(float* M, int Tn, int 
     if (tid == 0) {
       for (int t = 0; t < 16; ++t)
         if (sbTile(g, t))
-          tc::bulkStore(M + tileBase(Tn, g.I0 + (t >> 2), g.K0 + (t & 3)), opAddr + (uint32_t)t * kTileBytes,
+          tc::bulkStore(M + tileBase(Tn, g.I0 + (t >> 2), g.K0 + (t & 3)), cAddr + (uint32_t)t * kTileBytes,
                         kTileBytes);
       tc::bulkCommit();
-      tc::bulkWaitRead0();  // the stores have read the buffer: the next operands may land in it
-      if (sb + stride < nsb) issueOps(sbGeo(sb + stride, J, Tn));
+      tc::bulkWaitRead0();  // the stores have read the C buffer: the next C tiles may land in it
+      if (more) issueC(sbGeo(sb + stride, J, Tn));
     }
   }
   if (tid == 0) {
