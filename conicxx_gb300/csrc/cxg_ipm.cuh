@@ -1965,12 +1965,13 @@ __device__ __noinline__ bool gridLdltPairs(GridCtl* g, int nr, int nx, const Dev
 // Tiled right-looking LDL' of the root over the whole grid. Per tile column J:
 //  (A) the off-diagonal tiles of column J, one warp each; barrier;
 //  (B) the trailing update C_IK -= L_IJ D_J L_KJ^T, J < K <= I, in super-blocks of 4x4 tiles, one
-//      CTA each (superSyrk, CTAs 1..), while warp 0 of CTA 0 updates the tile (J+1, J+1) with the
-//      tile routine and factors it (one-column lookahead); barrier.
-// Every root entry receives its updates in increasing J with the same operations and rounding as
-// the single-CTA factor, so both give the same bits. Only warp 0 of CTA 0 factors diagonal tiles,
-// so the pivot statistics stay in CTA 0's shared memory (ps). `stage` holds gridStageBytes. The
-// double-float factor runs over column pairs instead (gridLdltStepsDf).
+//      CTA each (CTAs 1..: FP32 on the tensor cores, tcTrailingStep; FP64 and double-float on the
+//      CUDA cores, superSyrk), while warp 0 of CTA 0 updates the tile (J+1, J+1) with the tile
+//      routine and factors it (one-column lookahead); barrier.
+// In FP64 every root entry receives its updates in increasing J with the same operations and
+// rounding as the single-CTA factor, so both give the same bits. Only warp 0 of CTA 0 factors
+// diagonal tiles, so the pivot statistics stay in CTA 0's shared memory (ps). `stage` holds
+// gridStageBytes. Large FP32 and double-float roots run over column pairs instead (gridLdltPairs).
 template <typename T>
 __device__ __noinline__ bool gridLdltSteps(GridCtl* g, int nr, int nx, const DevSettings& st, T* M, PivotStats* ps,
                                            T* stage, unsigned char* slices, int Tn, int warp, int gw, int GW, bool cta0,
