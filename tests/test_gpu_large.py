@@ -61,9 +61,9 @@ def _probe(K, nx, b, arith, threads):
 def test_grid_factor_equals_one_cta(arith, nr, nx):
     """The whole-GPU LDL' is bit-identical to the one-CTA LDL' in FP64 (same tile operations in
     the same order per tile); in FP32 its trailing updates run on the tensor cores as 3xTF32
-    products, so L and D agree to FP32 accuracy, and in double-float as products of BF16 slices
-    exact to 2^-48 of the operands' row maxima, so L and D agree to 1e-11. Its solve agrees with
-    numpy to the arithmetic's accuracy. Sizes up to six tiles, the largest 8-byte root the
+    products, so L and D agree to FP32 accuracy; in double-float (at these sizes the one-column
+    form, whose trailing update runs on the CUDA cores) L and D agree to 1e-11. Its solve agrees
+    with numpy to the arithmetic's accuracy. Sizes up to six tiles, the largest 8-byte root the
     one-CTA probe holds in shared memory."""
     K = _quasi_definite(nr, nx, nr + 7)
     b = np.random.default_rng(nr).standard_normal(nr)
@@ -95,8 +95,7 @@ def test_grid_factor_large_root(arith):
     tol = {"fp64": 1e-10, "df64": 1e-8, "fp32": 1e-3}[arith]
     assert rel(x, xs) < tol
     # FP32 (tensor-core 3xTF32 trailing updates): the reconstruction at FP32 accuracy, well below
-    # the ~1e-3 of a single TF32 product; double-float (BF16-slice tensor-core products): at the
-    # level of an FP64 factor
+    # the ~1e-3 of a single TF32 product; double-float: at the level of an FP64 factor
     recon = rel(L @ np.diag(D) @ L.T, K)
     print(arith, "reconstruction", recon, "solve", rel(x, xs))
     assert recon < {"fp64": 1e-10, "df64": 1e-12, "fp32": 1e-5}[arith]
