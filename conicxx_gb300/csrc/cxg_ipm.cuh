@@ -1717,8 +1717,6 @@ static __device__ __noinline__ bool tcDfTrailingStep(df64* M, int Tn, int J, lon
 // ((o * 2 + p) * 16 + kg) * rows * 16 + m * 16: each (o, p, kg) plane is the canonical
 // shared-memory layout of cxg_tc.cuh for every row, so the 128 rows of a super-block are one
 // contiguous copy per plane.
-constexpr int kPairMinTilesF32 = 352;  // 11264 rows
-constexpr int kPairMinTilesDf = 160;   // 5120 rows
 constexpr int kF32Parts = 2;
 constexpr int kF32Groups = kDfK / 4;                                     // 16-byte k-groups per row
 constexpr uint32_t kF32PanelBytes = (uint32_t)tc::kRows * kDfK * 4;      // 32 KB: 128 x 64 TF32
@@ -1979,7 +1977,10 @@ __device__ __noinline__ bool gridLdltSteps(GridCtl* g, int nr, int nx, const Dev
 
 // Roots of at least this many tile columns factor over column pairs (gridLdltPairs): half the C
 // traffic of the trailing update, but a longer serial chain per pair. Below it, one column at a
-// time (gridLdltSteps: FP32 on the tensor cores, double-float on the CUDA cores).
+// time (gridLdltSteps: FP32 on the tensor cores, double-float on the CUDA cores). The thresholds
+// are the measured crossovers of the two forms on GB300.
+constexpr int kPairMinTilesF32 = 352;  // 11264 rows
+constexpr int kPairMinTilesDf = 160;   // 5120 rows
 template <typename T>
 __device__ __forceinline__ constexpr int pairMinTiles() {
   return (ArithOf<T>::v == 1) ? kPairMinTilesF32 : kPairMinTilesDf;
